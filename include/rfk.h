@@ -1,0 +1,246 @@
+/*
+ * rfk.h - C ABI of the GB300 flame-rendering hot path (librfk.so).
+ *
+ * Each entry point replaces one call of librefrakt's hot path; the reference
+ * interface it stands in for is cited beside it (paths relative to the
+ * reference project root). Conventions:
+ *   - every call returns an rfk_status (0 = RFK_OK); on failure the message is
+ *     available from rfk_last_error() on the calling thread, in place of the
+ *     reference's log + exit(1) (src/librefrakt/include/librefrakt/util/cuda.h:16-25);
+ *   - opaque handles are released with the matching *_destroy call;
+ *   - GPU work is enqueued on the caller's stream (a cudaStream_t passed as
+ *     void*, NULL = the legacy default stream); device pointers are CUDA
+ *     device addresses on the current device;
+ *   - handles are thread-compatible: one state per thread, kernels may be
+ *     shared, the compile cache is internally locked.
+ */
+#ifndef RFK_H
+#define RFK_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef int rfk_status;
+#define RFK_OK 0
+#define RFK_E_INVALID 1  /* bad argument or size */
+#define RFK_E_FORMAT 2   /* genome / database text that does not parse or validate */
+#define RFK_E_COMPILE 3  /* NVRTC or module load failure (log returned) */
+#define RFK_E_CUDA 4     /* CUDA runtime / driver error */
+#define RFK_E_NODEVICE 5 /* no usable sm_100-class device */
+
+typedef struct rfk_db rfk_db;
+typedef struct rfk_flame rfk_flame;
+typedef struct rfk_kernel rfk_kernel;
+typedef struct rfk_state rfk_state;
+
+/* Thread-local text of the last failure on this thread ("" if none). */
+const char* rfk_last_error(void);
+/* Library version, major * 10000 + minor * 100 + patch. */
+int rfk_version(void);
+
+/* ---- variation database ------------------------------------------------
+ * rfkt::initialize(flamedb&, config_path)  src/librefrakt/src/flame_info.cpp:60-148
+ * Loads <dir>/variations_new.yml and <dir>/common.yml. */
+rfk_status rfk_db_load(const char* config_dir, rfk_db** out);
+void rfk_db_destroy(rfk_db* db);
+/* flamedb::variations() / is_variation  flame_info.h:69-88 */
+int rfk_db_variation_count(const rfk_db* db);
+rfk_status rfk_db_variation_name(const rfk_db* db, int index, char* buf, size_t cap);
+/* flamedb::hash()  flame_info.h:131-133 */
+uint64_t rfk_db_hash(const rfk_db* db);
+/* Translated device source of one variation (diagnostics, host-twin tests). */
+rfk_status rfk_db_variation_source(const rfk_db* db, const char* name, char* buf, size_t cap, size_t* len);
+
+/* ---- genomes -------------------------------------------------------------
+ * rfkt::flame::deserialize  src/librefrakt/src/flame_types.cpp:437-485
+ * rfkt::import_flam3        src/librefrakt/src/flame_types.cpp:131-239
+ * flame::serialize           src/librefrakt/src/flame_types.cpp:399-435 (palette written as [h,s,v] triples) */
+rfk_status rfk_flame_from_json(const rfk_db* db, const char* json, rfk_flame** out);
+rfk_status rfk_flame_from_flam3(const rfk_db* db, const char* xml, rfk_flame** out);
+rfk_status rfk_flame_to_json(const rfk_flame* f, char* buf, size_t cap, size_t* len);
+void rfk_flame_destroy(rfk_flame* f);
+/* flame::size_reals()  src/librefrakt/include/librefrakt/flame_types.h:602-613 */
+size_t rfk_flame_size_reals(const rfk_flame* f);
+/* flame::pack_sample(packer, invoker, t, w, h)  flame_types.h:634-672.
+ * Writes size_reals + 768 doubles (static genome: every t gives t0 values). */
+rfk_status rfk_flame_pack_sample(const rfk_flame* f, int w, int h, double* out, size_t cap);
+/* flame::affine_indices()  flame_types.h:674-705 */
+rfk_status rfk_flame_affine_indices(const rfk_flame* f, size_t* out, size_t cap, size_t* count);
+/* gamma, brightness, vibrancy, highlight_power of the genome (flame_types.h:565-569). */
+rfk_status rfk_flame_tonemap_params(const rfk_flame* f, double out[4]);
+/* structure hash: equal hashes share a kernel (flame_types.h:578-592) */
+uint64_t rfk_flame_structure_hash(const rfk_flame* f);
+
+/* ---- per-flame kernels ---------------------------------------------------
+ * flame_compiler::get_flame_kernel(fdb, precision, flame) -> result
+ *   src/librefrakt/include/librefrakt/flame_compiler.h:156-182,
+ *   src/librefrakt/src/flame_compiler.cpp:601-656
+ * One NVRTC (sm_103a) module per (structure, options); changing genome values
+ * reuses it. Fields left 0 choose the defaults / the autotuned launch shape. */
+typedef struct {
+    int precise_math;      /* 0: -use_fast_math as the reference (flame_compiler.cpp:861); 1: full-precision libm */
+    int block;             /* threads per block (0 = 256) */
+    int chains_per_thread; /* 0 = 1 */
+    int flush;             /* histogram update: 0 = red.global.add.v4.f32 per draw, 1 = warp-aggregated */
+    int blocks_per_sm;     /* 0 = as many as fit */
+    int check_interval;    /* passes between bailout checks (0 = 32) */
+} rfk_compile_opts;
+
+typedef struct {
+    int grid;               /* persistent blocks = temporal samples */
+    int block;
+    int chains_per_thread;
+    int flush;
+    int registers;          /* of the bin kernel */
+    int num_xforms;
+    int has_final;
+    int chaos;
+    size_t size_reals;
+    size_t sample_floats;   /* floats per prepared parameter block */
+    double compile_ms;
+    double sfu_per_iter;    /* weighted transcendental calls per chain step */
+} rfk_kernel_info;
+
+rfk_status rfk_compile(const rfk_db* db, const rfk_flame* f, const rfk_compile_opts* opts, rfk_kernel** out,
+                       char* log, size_t log_cap);
+void rfk_kernel_destroy(rfk_kernel* k);
+rfk_status rfk_kernel_get_info(const rfk_kernel* k, rfk_kernel_info* out);
+/* Full NVRTC text for a flame (device prelude, generated flame code, kernel
+ * bodies); needs no device. */
+rfk_status rfk_generate_source(const rfk_db* db, const rfk_flame* f, char* buf, size_t cap, size_t* len);
+/* NVRTC-compiles the flame's kernels for `arch` (e.g. "sm_103a") without
+ * loading them: a compile check that needs no device. */
+rfk_status rfk_compile_check(const rfk_db* db, const rfk_flame* f, const rfk_compile_opts* opts, const char* arch, char* log,
+                             size_t log_cap);
+/* The generated device source (flame_compiler::result::source). */
+rfk_status rfk_kernel_source(const rfk_kernel* k, char* buf, size_t cap, size_t* len);
+
+/* ---- render state ----------------------------------------------------------
+ * flame_kernel::warmup(stream, samples, dims, seed, count, temporal_multiplier)
+ *   flame_compiler.h:99-100, flame_compiler.cpp:1037-1108
+ * samples: host array of nsamples x (size_reals + 768) doubles (pack_sample
+ * output, nsamples >= 4); the spline segments between samples 1 and
+ * nsamples-2 are spread over the persistent blocks as temporal samples. The
+ * state owns a cleared w x h float4 histogram (device), chain states and
+ * counters. temporal_multiplier must be 1. */
+rfk_status rfk_warmup(const rfk_kernel* k, const double* samples, size_t nsamples, uint32_t w, uint32_t h,
+                      uint32_t seed, uint32_t warmup_count, int temporal_multiplier, void* stream, rfk_state** out);
+void rfk_state_destroy(rfk_state* s);
+
+/* flame_kernel::bailout_args  flame_compiler.h:92-96 */
+typedef struct {
+    uint32_t iters;   /* passes per chain cap for this call (0 = none) */
+    uint32_t millis;  /* time budget (0 = none) */
+    double quality;   /* additional spp to reach (0 = none) */
+} rfk_bailout;
+
+/* flame_kernel::bin_result  flame_compiler.h:27-35 (+ status bits and draw count) */
+typedef struct {
+    double quality;           /* spp added by this call: sum(255 * opacity) / (255 * pixels) */
+    double elapsed_ms;        /* kernel span from %globaltimer */
+    uint64_t total_passes;    /* chain steps */
+    uint64_t total_draws;     /* sum(255 * opacity) / 255, as the reference reports */
+    uint64_t total_bins;      /* pixels */
+    double passes_per_thread;
+    double max_density;
+    uint64_t draw_count;      /* in-bounds draws with opacity > 0 */
+    uint32_t status;          /* 1 quality reached, 2 time, 4 stopped, 8 pass cap */
+} rfk_bin_result;
+
+/* flame_kernel::bin(stream, state, bailout, temporal_slicing)
+ *   flame_compiler.h:98, flame_compiler.cpp:866-955
+ * rfk_bin enqueues and waits; rfk_bin_async enqueues, rfk_bin_wait waits for
+ * the last enqueued call's result. Repeated calls keep accumulating. */
+rfk_status rfk_bin(rfk_state* s, const rfk_bailout* bo, void* stream, rfk_bin_result* out);
+rfk_status rfk_bin_async(rfk_state* s, const rfk_bailout* bo, void* stream);
+rfk_status rfk_bin_wait(rfk_state* s, rfk_bin_result* out);
+/* saved_state::abort_binning()  flame_compiler.h:85-88: safe from any thread. */
+rfk_status rfk_state_abort(rfk_state* s);
+/* Device pointer of the float4 histogram (w * h * 4 floats, row-major). */
+float* rfk_state_bins(rfk_state* s);
+/* Accumulated spp over all bin calls (saved_state::quality). */
+double rfk_state_quality(const rfk_state* s);
+/* Chain states copied to the host: x, y, colour (each `count` floats). */
+rfk_status rfk_state_chains(rfk_state* s, float* x, float* y, float* c, size_t cap, size_t* count);
+/* Prepared per-sample parameter blocks copied to the host (grid x sample_floats floats). */
+rfk_status rfk_state_samples(rfk_state* s, float* out, size_t cap, size_t* count);
+
+/* ---- single map application (parity unit) -------------------------------
+ * Applies xform `xform` (-1 = final) of one prepared parameter block (host,
+ * sample_floats floats) to n points (x, y, colour) -> (x, y, colour, opacity).
+ * Uses the xform dispatch of flame.tpl:146-160. Host in, host out. */
+rfk_status rfk_apply_xform(const rfk_kernel* k, const float* params, int xform, const float* in_xyc, size_t n,
+                           float* out_xyco, uint32_t seed);
+/* Prepared parameter blocks for explicit (segment, t) pairs, host in / out:
+ * samples as for rfk_warmup; seg[i], t[i] for i < count; out count x sample_floats. */
+rfk_status rfk_prepare_samples(const rfk_kernel* k, const double* samples, size_t nsamples, const uint32_t* seg,
+                               const float* t, size_t count, uint32_t seed, float* out);
+
+/* ---- image steps ----------------------------------------------------------
+ * tonemapper::run(bins, out, args, stream)
+ *   src/librefrakt/include/librefrakt/image/tonemapper.h:10-22,
+ *   src/librefrakt/src/image/tonemapper.cpp:37-56, assets/kernels/tonemap.cu:50-105 */
+#define RFK_HALF3 0
+#define RFK_HALF4 1
+#define RFK_FLOAT3 2
+#define RFK_FLOAT4 3
+typedef struct {
+    double quality;          /* accumulated spp */
+    double gamma;
+    double brightness;
+    double vibrancy;
+    double max_density;      /* accepted for interface parity; unused, as in the reference */
+    double highlight_power;  /* < 0 = off (reference behaviour); >= 0 flam3-style highlight desaturation */
+    int precise;             /* 1 = full-precision log/pow; 0 = the reference kernel's fast intrinsics */
+} rfk_tonemap_args;
+/* bins: device float4[w*h]; out: device image of the given format.
+ * histogram / max_density (device, may be NULL): when given, the density
+ * histogram of density_histo.cu:1-42 (97 u64 bins, granularity 4) and the max
+ * density are accumulated in the same pass; the caller clears them first. */
+rfk_status rfk_tonemap(const float* bins, uint32_t w, uint32_t h, void* out, int format, const rfk_tonemap_args* args,
+                       uint64_t* histogram, uint64_t* max_density, void* stream);
+
+/* calculate_histogram<4>  assets/kernels/density_histo.cu:1-42 (launched by
+ * flame_kernel::bin, flame_compiler.cpp:928-937). Device pointers; the caller
+ * clears histogram[97] and max_density. */
+rfk_status rfk_density_histogram(const float* bins, uint32_t count, uint64_t* histogram, uint64_t* max_density,
+                                 void* stream);
+
+/* Density-estimation blur (no reference counterpart: the reference README
+ * src/librefrakt/README.md:14 replaces it by a denoiser). Device float4 in / out
+ * (distinct buffers), radius = clamp(max_radius * density^-curve, min_radius,
+ * max_radius), max_radius <= 9. */
+typedef struct {
+    double max_radius;
+    double min_radius;
+    double curve;
+} rfk_de_args;
+rfk_status rfk_density_blur(const float* bins_in, float* bins_out, uint32_t w, uint32_t h, const rfk_de_args* args,
+                            void* stream);
+
+/* generate_sample_coefficients  assets/kernels/catmull.cu:33-42: device FP64
+ * samples [nseg + 3][sample_size] -> device FP32 coefficients
+ * [nseg][sample_size][4] (a, b, c, d of a t^3 + b t^2 + c t + d). */
+rfk_status rfk_catmull_coefficients(const double* samples, uint32_t sample_size, uint32_t nseg, float* coeff,
+                                    void* stream);
+
+/* fix_rotation  src/librefrakt/src/flame_compiler.cpp:957-1035, host, in place. */
+rfk_status rfk_fix_rotation(double* samples, size_t nsamples, size_t sample_size, size_t flame_size,
+                            const size_t* affine_indices, size_t n_affine);
+
+/* ---- measurement helpers -------------------------------------------------- */
+/* red.global.add.v4.f32 operations per second into a device buffer of
+ * `bytes` (random slots): the L2-atomic roofline. */
+rfk_status rfk_probe_red_v4(size_t bytes, uint32_t iters_per_thread, double* ops_per_s);
+/* Number of SMs of the current device. */
+int rfk_device_sm_count(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* RFK_H */

@@ -1,0 +1,832 @@
+// librfk runtime: NVRTC flame kernels, render states, image steps, C ABI.
+//
+// Host-side counterpart of flame_compiler / flame_kernel / tonemapper
+// (src/librefrakt/src/flame_compiler.cpp, src/librefrakt/src/image/tonemapper.cpp),
+// using the CUDA runtime for memory and streams and the driver API for the
+// NVRTC-built modules. Failures return a status with a thread-local message
+// instead of logging and exiting.
+#include <cuda_runtime.h>
+#include <nvrtc.h>
+
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstring>
+#include <map>
+#include <memory>
+#include <mutex>
+#include <sstream>
+#include <string>
+#include <vector>
+
+#include "../../../include/rfk.h"
+#include "../kernels/image_kernels.h"
+#include "codegen.h"
+#include "flamedb.h"
+#include "genome.h"
+
+extern const char* const rfk_src_device;
+extern const char* const rfk_src_iterate;
+
+namespace {
+
+thread_local std::string g_error;
+
+struct rfk_exception : std::runtime_error {
+    rfk_status code;
+    rfk_exception(rfk_status c, const std::string& m) : std::runtime_error(m), code(c) {}
+};
+
+[[noreturn]] void fail(rfk_status c, const std::string& m) { throw rfk_exception(c, m); }
+
+void cuda_check(cudaError_t e, const char* what) {
+    if (e != cudaSuccess) fail(RFK_E_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+
+template <typename F>
+rfk_status guard(F&& f) {
+    try {
+        g_error.clear();
+        f();
+        return RFK_OK;
+    } catch (const rfk_exception& e) {
+        g_error = e.what();
+        return e.code;
+    } catch (const rfk::format_error& e) {
+        g_error = e.what();
+        return RFK_E_FORMAT;
+    } catch (const rfk::dsl::parse_error& e) {
+        g_error = e.what();
+        return RFK_E_FORMAT;
+    } catch (const std::bad_alloc&) {
+        g_error = "out of host memory";
+        return RFK_E_INVALID;
+    } catch (const std::exception& e) {
+        g_error = e.what();
+        return RFK_E_INVALID;
+    }
+}
+
+int device_sm_count() {
+    int dev = 0, n = 0;
+    cuda_check(cudaGetDevice(&dev), "cudaGetDevice");
+    cuda_check(cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev), "cudaDeviceGetAttribute");
+    return n;
+}
+
+std::string device_arch() {
+    int dev = 0, major = 0, minor = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) fail(RFK_E_NODEVICE, std::string("no CUDA device: ") + cudaGetErrorString(e));
+    cuda_check(cudaDeviceGetAttribute(&major, cudaDevAttrComputeCapabilityMajor, dev), "compute capability");
+    cuda_check(cudaDeviceGetAttribute(&minor, cudaDevAttrComputeCapabilityMinor, dev), "compute capability");
+    if (major < 10) fail(RFK_E_NODEVICE, "device compute capability " + std::to_string(major) + "." + std::to_string(minor) +
+                                             " is below the sm_100 family this library targets");
+    return "sm_" + std::to_string(major) + std::to_string(minor) + "a";
+}
+
+// Host mirror of rfk_chains / rfk_bin_args / rfk_counters in rfk_iterate.cuh.
+struct dev_chains {
+    float* x;
+    float* y;
+    float* c;
+    unsigned char* last;
+};
+struct dev_bin_args {
+    const float* samples;
+    dev_chains st;
+    float4* bins;
+    unsigned w, h;
+    unsigned seed, salt;
+    unsigned call_id, pad0;
+    unsigned long long quality_target;
+    unsigned long long max_passes;
+    unsigned long long time_ns;
+    const volatile unsigned* stop;
+    unsigned long long* counters;
+};
+constexpr int kCounterWords = 6;  // quality, passes, start, stop, draws, status|pad
+
+}  // namespace
+
+// ------------------------------------------------------------------ handles --
+struct rfk_db {
+    rfk::flamedb db;
+};
+
+struct rfk_flame {
+    rfk::flame f;
+};
+
+struct kernel_impl {
+    rfk::generated_flame gen;
+    std::string source;
+    std::string log;
+    cudaLibrary_t lib = nullptr;
+    cudaKernel_t f_prepare = nullptr, f_warmup = nullptr, f_bin = nullptr, f_apply = nullptr;
+    int block = 256, cpt = 1, flush = 0, grid = 0, regs = 0, check = 32;
+    size_t sample_floats = 0;
+    double compile_ms = 0.0;
+    double sfu_per_iter = 0.0;
+    uint32_t salt = 0;
+    ~kernel_impl() {
+        if (lib) cudaLibraryUnload(lib);
+    }
+};
+
+struct rfk_kernel {
+    std::shared_ptr<kernel_impl> impl;
+};
+
+struct rfk_state {
+    std::shared_ptr<const kernel_impl> k;
+    unsigned w = 0, h = 0, seed = 0;
+    int grid = 0;
+    size_t nchains = 0;
+    float* d_samples = nullptr;
+    float *d_x = nullptr, *d_y = nullptr, *d_c = nullptr;
+    unsigned char* d_last = nullptr;
+    float4* d_bins = nullptr;
+    unsigned long long* d_counters = nullptr;  // kCounterWords + 98 (histogram + max density)
+    unsigned long long* h_counters = nullptr;  // pinned mirror
+    unsigned* h_stop = nullptr;                // mapped pinned
+    unsigned* d_stop = nullptr;
+    cudaEvent_t done = nullptr;
+    unsigned call_id = 0;
+    double quality = 0.0;
+    unsigned long long warmup_hits = 0;
+    bool pending = false;
+
+    ~rfk_state() {
+        if (done) cudaEventSynchronize(done);
+        for (void* p : {(void*)d_samples, (void*)d_x, (void*)d_y, (void*)d_c, (void*)d_last, (void*)d_bins, (void*)d_counters})
+            if (p) cudaFree(p);
+        if (h_counters) cudaFreeHost(h_counters);
+        if (h_stop) cudaFreeHost(h_stop);
+        if (done) cudaEventDestroy(done);
+    }
+};
+
+namespace {
+
+size_t sample_floats_for(const rfk::generated_flame& g) {
+    size_t off = g.size_reals + g.num_xforms + 1;
+    if (g.chaos) off += g.num_xforms * g.num_xforms + g.num_xforms;
+    off = (off + 3) / 4 * 4;
+    return off + 1024;
+}
+
+std::string full_source(const rfk::generated_flame& g) {
+    std::ostringstream src;
+    src << rfk_src_device << "\n" << g.source << "\n" << rfk_src_iterate << "\n";
+    return src.str();
+}
+
+std::vector<char> nvrtc_build(const std::string& source, const std::string& arch_name, const rfk_compile_opts& o, int block,
+                              int cpt, int flush, int check, std::string& log) {
+    const std::string arch = "--gpu-architecture=" + arch_name;
+    const std::string d_block = "-DRFK_BLOCK=" + std::to_string(block);
+    const std::string d_cpt = "-DRFK_CPT=" + std::to_string(cpt);
+    const std::string d_flush = "-DRFK_FLUSH=" + std::to_string(flush);
+    const std::string d_check = "-DRFK_CHECK=" + std::to_string(check);
+    std::vector<const char*> opts = {arch.c_str(), "-std=c++17", "-lineinfo", d_block.c_str(), d_cpt.c_str(),
+                                     d_flush.c_str(), d_check.c_str(), "-extra-device-vectorization"};
+    if (!o.precise_math) opts.push_back("--use_fast_math");
+    nvrtcProgram prog;
+    if (nvrtcCreateProgram(&prog, source.c_str(), "rfk_flame.cu", 0, nullptr, nullptr) != NVRTC_SUCCESS)
+        fail(RFK_E_COMPILE, "nvrtcCreateProgram failed");
+    nvrtcResult cr = nvrtcCompileProgram(prog, (int)opts.size(), opts.data());
+    size_t log_size = 0;
+    nvrtcGetProgramLogSize(prog, &log_size);
+    std::string nlog(log_size, '\0');
+    if (log_size) nvrtcGetProgramLog(prog, nlog.data());
+    while (!nlog.empty() && nlog.back() == '\0') nlog.pop_back();
+    log = nlog;
+    if (cr != NVRTC_SUCCESS) {
+        nvrtcDestroyProgram(&prog);
+        fail(RFK_E_COMPILE, std::string("NVRTC: ") + nvrtcGetErrorString(cr) + "\n" + nlog);
+    }
+    size_t cubin_size = 0;
+    nvrtcGetCUBINSize(prog, &cubin_size);
+    std::vector<char> cubin(cubin_size);
+    nvrtcGetCUBIN(prog, cubin.data());
+    nvrtcDestroyProgram(&prog);
+    return cubin;
+}
+
+void check_options(const rfk_compile_opts& o) {
+    const int block = o.block > 0 ? o.block : 256;
+    if (block % 32 != 0 || block > 1024) fail(RFK_E_INVALID, "block must be a multiple of 32 up to 1024");
+    if (o.chains_per_thread > 8 || o.chains_per_thread < 0) fail(RFK_E_INVALID, "chains_per_thread must be in [0, 8]");
+    if (o.flush < 0 || o.flush > 1) fail(RFK_E_INVALID, "flush must be 0 or 1");
+    if (o.check_interval < 0 || o.blocks_per_sm < 0) fail(RFK_E_INVALID, "negative option");
+}
+
+// NVRTC module cache: (db hash, structure, options) -> kernel.
+std::mutex g_cache_mu;
+std::map<std::string, std::weak_ptr<kernel_impl>> g_cache;
+
+std::shared_ptr<kernel_impl> compile(const rfk::flamedb& db, const rfk::flame& f, const rfk_compile_opts& o, std::string& log) {
+    const auto t0 = std::chrono::steady_clock::now();
+    auto k = std::make_shared<kernel_impl>();
+    k->gen = rfk::generate_flame_code(db, f);
+    k->block = o.block > 0 ? o.block : 256;
+    k->cpt = o.chains_per_thread > 0 ? o.chains_per_thread : 1;
+    k->flush = o.flush;
+    k->check = o.check_interval > 0 ? o.check_interval : 32;
+    check_options(o);
+    k->sample_floats = sample_floats_for(k->gen);
+    if (k->sample_floats * 4 > 44 * 1024) fail(RFK_E_INVALID, "flame too large for the shared-memory parameter block");
+    k->salt = (uint32_t)(f.structure_hash() ^ (f.structure_hash() >> 32));
+
+    k->source = full_source(k->gen);
+
+    std::vector<char> cubin = nvrtc_build(k->source, device_arch(), o, k->block, k->cpt, k->flush, k->check, log);
+    cuda_check(cudaLibraryLoadData(&k->lib, cubin.data(), nullptr, nullptr, 0, nullptr, nullptr, 0), "cudaLibraryLoadData");
+    cuda_check(cudaLibraryGetKernel(&k->f_prepare, k->lib, "rfk_prepare"), "rfk_prepare");
+    cuda_check(cudaLibraryGetKernel(&k->f_warmup, k->lib, "rfk_warmup"), "rfk_warmup");
+    cuda_check(cudaLibraryGetKernel(&k->f_bin, k->lib, "rfk_bin"), "rfk_bin");
+    cuda_check(cudaLibraryGetKernel(&k->f_apply, k->lib, "rfk_apply"), "rfk_apply");
+    cudaFuncAttributes fa{};
+    cuda_check(cudaFuncGetAttributes(&fa, reinterpret_cast<const void*>(k->f_bin)), "attributes");
+    k->regs = fa.numRegs;
+    int per_sm = 0;
+    cuda_check(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, reinterpret_cast<const void*>(k->f_bin), k->block, 0),
+               "occupancy");
+    if (per_sm < 1) fail(RFK_E_COMPILE, "bin kernel cannot be resident with block " + std::to_string(k->block));
+    if (o.blocks_per_sm > 0) per_sm = std::min(per_sm, o.blocks_per_sm);
+    k->grid = per_sm * device_sm_count();
+
+    // weighted transcendental count per chain step
+    double wsum = 0.0;
+    for (auto& xf : f.xforms) wsum += xf.weight;
+    double sfu = 0.0;
+    for (size_t i = 0; i < f.xforms.size(); i++)
+        sfu += (wsum > 0 ? f.xforms[i].weight / wsum : 0.0) * k->gen.xforms[i].sfu_ops;
+    if (k->gen.has_final) sfu += k->gen.xforms.back().sfu_ops;
+    k->sfu_per_iter = sfu;
+    k->compile_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+    return k;
+}
+
+std::shared_ptr<kernel_impl> compile_cached(const rfk::flamedb& db, const rfk::flame& f, const rfk_compile_opts& o,
+                                           std::string& log) {
+    std::ostringstream key;
+    key << db.hash() << "|" << f.structure_key() << "|" << o.precise_math << "," << o.block << "," << o.chains_per_thread
+        << "," << o.flush << "," << o.blocks_per_sm << "," << o.check_interval;
+    {
+        std::lock_guard<std::mutex> lk(g_cache_mu);
+        auto it = g_cache.find(key.str());
+        if (it != g_cache.end())
+            if (auto sp = it->second.lock()) return sp;
+    }
+    auto k = compile(db, f, o, log);
+    std::lock_guard<std::mutex> lk(g_cache_mu);
+    g_cache[key.str()] = k;
+    return k;
+}
+
+void launch(cudaKernel_t fn, unsigned grid, unsigned block, cudaStream_t s, void** args, const char* what) {
+    cuda_check(cudaLaunchKernel(reinterpret_cast<const void*>(fn), dim3(grid), dim3(block), args, 0, s), what);
+}
+
+// Temporal sample s of S: spline segment and t within it, as refactor.cu:266-270.
+void temporal_schedule(unsigned S, unsigned nseg, std::vector<unsigned>& seg, std::vector<float>& t) {
+    if (nseg == 0) fail(RFK_E_INVALID, "need at least 4 samples");
+    if (S < nseg) fail(RFK_E_INVALID, "fewer temporal samples than spline segments");
+    const unsigned seg_size = S / nseg;
+    seg.resize(S);
+    t.resize(S);
+    for (unsigned s = 0; s < S; s++) {
+        unsigned sg = s / seg_size;
+        float tt = (float)(s % seg_size) / (float)(S / nseg);
+        if (sg >= nseg) {
+            sg = nseg - 1;
+            tt = 1.0f;
+        }
+        seg[s] = sg;
+        t[s] = tt;
+    }
+}
+
+// Uploads samples (after fix_rotation), builds spline coefficients and runs
+// the prepare kernel for the given schedule into d_out (count x sample_floats).
+void prepare(const kernel_impl& k, const double* samples, size_t nsamples, const std::vector<unsigned>& seg,
+             const std::vector<float>& t, unsigned seed, float* d_out, cudaStream_t s) {
+    const size_t sample_size = k.gen.size_reals + rfk::palette_reals;
+    if (nsamples < 4) fail(RFK_E_INVALID, "need at least 4 packed samples");
+    std::vector<double> host(samples, samples + nsamples * sample_size);
+    rfk::fix_rotation(host, sample_size, k.gen.size_reals, k.gen.affine_indices);
+    const unsigned nseg = (unsigned)(nsamples - 3);
+    for (unsigned sg : seg)
+        if (sg >= nseg) fail(RFK_E_INVALID, "segment index out of range");
+    double* d_samples = nullptr;
+    float4* d_coeff = nullptr;
+    unsigned* d_seg = nullptr;
+    float* d_t = nullptr;
+    cuda_check(cudaMallocAsync(&d_samples, host.size() * sizeof(double), s), "alloc samples");
+    cuda_check(cudaMallocAsync(&d_coeff, (size_t)nseg * sample_size * sizeof(float4), s), "alloc coefficients");
+    cuda_check(cudaMallocAsync(&d_seg, seg.size() * sizeof(unsigned), s), "alloc schedule");
+    cuda_check(cudaMallocAsync(&d_t, t.size() * sizeof(float), s), "alloc schedule");
+    cuda_check(cudaMemcpyAsync(d_samples, host.data(), host.size() * sizeof(double), cudaMemcpyHostToDevice, s), "H2D samples");
+    cuda_check(cudaMemcpyAsync(d_seg, seg.data(), seg.size() * sizeof(unsigned), cudaMemcpyHostToDevice, s), "H2D schedule");
+    cuda_check(cudaMemcpyAsync(d_t, t.data(), t.size() * sizeof(float), cudaMemcpyHostToDevice, s), "H2D schedule");
+    cuda_check(rfk_launch_catmull(d_samples, (unsigned)sample_size, nseg, d_coeff, s), "catmull");
+    unsigned ss = (unsigned)sample_size, salt = k.salt;
+    void* args[] = {&d_coeff, &ss, &d_seg, &d_t, &d_out, &seed, &salt};
+    launch(k.f_prepare, (unsigned)seg.size(), 256, s, args, "rfk_prepare");
+    // the host vectors must outlive the copies
+    cuda_check(cudaStreamSynchronize(s), "prepare");
+    cudaFreeAsync(d_samples, s);
+    cudaFreeAsync(d_coeff, s);
+    cudaFreeAsync(d_seg, s);
+    cudaFreeAsync(d_t, s);
+}
+
+void copy_out(char* buf, size_t cap, size_t* len, const std::string& s) {
+    if (len) *len = s.size();
+    if (buf && cap) {
+        size_t n = std::min(cap - 1, s.size());
+        std::memcpy(buf, s.data(), n);
+        buf[n] = '\0';
+    }
+}
+
+}  // namespace
+
+// ====================================================================== C ABI
+extern "C" {
+
+const char* rfk_last_error(void) { return g_error.c_str(); }
+int rfk_version(void) { return 100; }
+
+rfk_status rfk_db_load(const char* dir, rfk_db** out) {
+    return guard([&] {
+        if (!dir || !out) fail(RFK_E_INVALID, "null argument");
+        auto db = std::make_unique<rfk_db>();
+        rfk::load_flamedb(db->db, dir);
+        *out = db.release();
+    });
+}
+
+void rfk_db_destroy(rfk_db* db) { delete db; }
+
+int rfk_db_variation_count(const rfk_db* db) { return db ? (int)db->db.variations().size() : 0; }
+
+rfk_status rfk_db_variation_name(const rfk_db* db, int index, char* buf, size_t cap) {
+    return guard([&] {
+        if (!db || index < 0 || index >= (int)db->db.variations().size()) fail(RFK_E_INVALID, "bad variation index");
+        auto it = db->db.variations().begin();
+        std::advance(it, index);
+        copy_out(buf, cap, nullptr, it->first);
+    });
+}
+
+uint64_t rfk_db_hash(const rfk_db* db) { return db ? db->db.hash() : 0; }
+
+rfk_status rfk_db_variation_source(const rfk_db* db, const char* name, char* buf, size_t cap, size_t* len) {
+    return guard([&] {
+        if (!db || !name) fail(RFK_E_INVALID, "null argument");
+        if (!db->db.is_variation(name)) fail(RFK_E_INVALID, std::string("unknown variation ") + name);
+        const auto& def = db->db.get_variation(name);
+        rfk::dsl::emit_env env;
+        env.variation = name;
+        for (auto& [pn, _] : def.params) env.param_expr[pn] = "P_" + pn;
+        std::string s = rfk::dsl::emit_body(*def.apply_ast, env);
+        if (def.precalc_ast) {
+            rfk::dsl::emit_env penv = env;
+            penv.precalc = true;
+            s += "// precalc\n" + rfk::dsl::emit_body(*def.precalc_ast, penv);
+        }
+        copy_out(buf, cap, len, s);
+    });
+}
+
+rfk_status rfk_flame_from_json(const rfk_db* db, const char* json, rfk_flame** out) {
+    return guard([&] {
+        if (!db || !json || !out) fail(RFK_E_INVALID, "null argument");
+        auto f = std::make_unique<rfk_flame>();
+        f->f = rfk::flame_from_json(db->db, rfk::parse_json(json));
+        *out = f.release();
+    });
+}
+
+rfk_status rfk_flame_from_flam3(const rfk_db* db, const char* xml, rfk_flame** out) {
+    return guard([&] {
+        if (!db || !xml || !out) fail(RFK_E_INVALID, "null argument");
+        auto f = std::make_unique<rfk_flame>();
+        f->f = rfk::flame_from_flam3(db->db, xml);
+        *out = f.release();
+    });
+}
+
+rfk_status rfk_flame_to_json(const rfk_flame* f, char* buf, size_t cap, size_t* len) {
+    return guard([&] {
+        if (!f) fail(RFK_E_INVALID, "null flame");
+        copy_out(buf, cap, len, rfk::write_json(rfk::flame_to_json(f->f)));
+    });
+}
+
+void rfk_flame_destroy(rfk_flame* f) { delete f; }
+
+size_t rfk_flame_size_reals(const rfk_flame* f) { return f ? f->f.size_reals() : 0; }
+
+rfk_status rfk_flame_pack_sample(const rfk_flame* f, int w, int h, double* out, size_t cap) {
+    return guard([&] {
+        if (!f || !out) fail(RFK_E_INVALID, "null argument");
+        if (w <= 0 || h <= 0) fail(RFK_E_INVALID, "image size must be positive");
+        std::vector<double> v;
+        f->f.pack_sample(v, w, h);
+        if (cap < v.size()) fail(RFK_E_INVALID, "output buffer too small: need " + std::to_string(v.size()));
+        std::memcpy(out, v.data(), v.size() * sizeof(double));
+    });
+}
+
+rfk_status rfk_flame_affine_indices(const rfk_flame* f, size_t* out, size_t cap, size_t* count) {
+    return guard([&] {
+        if (!f) fail(RFK_E_INVALID, "null flame");
+        auto v = f->f.affine_indices();
+        if (count) *count = v.size();
+        if (out) {
+            if (cap < v.size()) fail(RFK_E_INVALID, "output buffer too small");
+            std::copy(v.begin(), v.end(), out);
+        }
+    });
+}
+
+rfk_status rfk_flame_tonemap_params(const rfk_flame* f, double out[4]) {
+    return guard([&] {
+        if (!f || !out) fail(RFK_E_INVALID, "null argument");
+        out[0] = f->f.gamma;
+        out[1] = f->f.brightness;
+        out[2] = f->f.vibrancy;
+        out[3] = f->f.highlight_power;
+    });
+}
+
+uint64_t rfk_flame_structure_hash(const rfk_flame* f) { return f ? f->f.structure_hash() : 0; }
+
+rfk_status rfk_compile(const rfk_db* db, const rfk_flame* f, const rfk_compile_opts* opts, rfk_kernel** out, char* log,
+                       size_t log_cap) {
+    std::string nlog;
+    rfk_status st = guard([&] {
+        if (!db || !f || !out) fail(RFK_E_INVALID, "null argument");
+        rfk_compile_opts o{};
+        if (opts) o = *opts;
+        auto k = compile_cached(db->db, f->f, o, nlog);
+        // handles share the cached module
+        *out = new rfk_kernel{k};
+    });
+    if (log && log_cap) copy_out(log, log_cap, nullptr, st == RFK_OK ? nlog : g_error);
+    return st;
+}
+
+}  // extern "C"
+
+namespace {
+const kernel_impl& K(const rfk_kernel* h) {
+    if (!h || !h->impl) fail(RFK_E_INVALID, "null kernel");
+    return *h->impl;
+}
+std::shared_ptr<kernel_impl> Kshared(const rfk_kernel* h) {
+    if (!h || !h->impl) fail(RFK_E_INVALID, "null kernel");
+    return h->impl;
+}
+}  // namespace
+
+extern "C" {
+
+void rfk_kernel_destroy(rfk_kernel* k) { delete k; }
+
+rfk_status rfk_generate_source(const rfk_db* db, const rfk_flame* f, char* buf, size_t cap, size_t* len) {
+    return guard([&] {
+        if (!db || !f) fail(RFK_E_INVALID, "null argument");
+        copy_out(buf, cap, len, full_source(rfk::generate_flame_code(db->db, f->f)));
+    });
+}
+
+rfk_status rfk_compile_check(const rfk_db* db, const rfk_flame* f, const rfk_compile_opts* opts, const char* arch, char* log,
+                             size_t log_cap) {
+    std::string nlog;
+    rfk_status st = guard([&] {
+        if (!db || !f || !arch) fail(RFK_E_INVALID, "null argument");
+        rfk_compile_opts o{};
+        if (opts) o = *opts;
+        check_options(o);
+        auto g = rfk::generate_flame_code(db->db, f->f);
+        nvrtc_build(full_source(g), arch, o, o.block > 0 ? o.block : 256, o.chains_per_thread > 0 ? o.chains_per_thread : 1,
+                    o.flush, o.check_interval > 0 ? o.check_interval : 32, nlog);
+    });
+    if (log && log_cap) copy_out(log, log_cap, nullptr, st == RFK_OK ? nlog : g_error);
+    return st;
+}
+
+rfk_status rfk_kernel_get_info(const rfk_kernel* kh, rfk_kernel_info* out) {
+    return guard([&] {
+        const kernel_impl& k = K(kh);
+        if (!out) fail(RFK_E_INVALID, "null output");
+        out->grid = k.grid;
+        out->block = k.block;
+        out->chains_per_thread = k.cpt;
+        out->flush = k.flush;
+        out->registers = k.regs;
+        out->num_xforms = (int)k.gen.num_xforms;
+        out->has_final = k.gen.has_final;
+        out->chaos = k.gen.chaos;
+        out->size_reals = k.gen.size_reals;
+        out->sample_floats = k.sample_floats;
+        out->compile_ms = k.compile_ms;
+        out->sfu_per_iter = k.sfu_per_iter;
+    });
+}
+
+rfk_status rfk_kernel_source(const rfk_kernel* kh, char* buf, size_t cap, size_t* len) {
+    return guard([&] { copy_out(buf, cap, len, K(kh).gen.source); });
+}
+
+rfk_status rfk_warmup(const rfk_kernel* kh, const double* samples, size_t nsamples, uint32_t w, uint32_t h, uint32_t seed,
+                      uint32_t warmup_count, int temporal_multiplier, void* stream, rfk_state** out) {
+    return guard([&] {
+        auto k = Kshared(kh);
+        if (!samples || !out) fail(RFK_E_INVALID, "null argument");
+        if (w == 0 || h == 0) fail(RFK_E_INVALID, "image size must be positive");
+        if ((uint64_t)w * h > (1ull << 31)) fail(RFK_E_INVALID, "image too large");
+        if (temporal_multiplier != 1) fail(RFK_E_INVALID, "temporal_multiplier must be 1");
+        cudaStream_t s = (cudaStream_t)stream;
+        auto st = std::make_unique<rfk_state>();
+        st->k = k;
+        st->w = w;
+        st->h = h;
+        st->seed = seed;
+        st->grid = k->grid;
+        st->nchains = (size_t)k->grid * k->block * k->cpt;
+        std::vector<unsigned> seg;
+        std::vector<float> t;
+        temporal_schedule((unsigned)st->grid, (unsigned)(nsamples - 3), seg, t);
+        cuda_check(cudaMalloc(&st->d_samples, (size_t)st->grid * k->sample_floats * sizeof(float)), "alloc samples");
+        prepare(*k, samples, nsamples, seg, t, seed, st->d_samples, s);
+        cuda_check(cudaMalloc(&st->d_x, st->nchains * sizeof(float)), "alloc chains");
+        cuda_check(cudaMalloc(&st->d_y, st->nchains * sizeof(float)), "alloc chains");
+        cuda_check(cudaMalloc(&st->d_c, st->nchains * sizeof(float)), "alloc chains");
+        cuda_check(cudaMalloc(&st->d_last, st->nchains), "alloc chains");
+        cuda_check(cudaMemsetAsync(st->d_last, 255, st->nchains, s), "init chains");
+        cuda_check(cudaMalloc(&st->d_bins, (size_t)w * h * sizeof(float4)), "alloc histogram");
+        cuda_check(cudaMemsetAsync(st->d_bins, 0, (size_t)w * h * sizeof(float4), s), "clear histogram");
+        cuda_check(cudaMalloc(&st->d_counters, (kCounterWords + 98) * sizeof(unsigned long long)), "alloc counters");
+        cuda_check(cudaMemsetAsync(st->d_counters, 0, (kCounterWords + 98) * sizeof(unsigned long long), s), "clear counters");
+        cuda_check(cudaHostAlloc(&st->h_counters, (kCounterWords + 98) * sizeof(unsigned long long), cudaHostAllocDefault), "pinned");
+        cuda_check(cudaHostAlloc(&st->h_stop, sizeof(unsigned), cudaHostAllocMapped), "stop flag");
+        *st->h_stop = 0;
+        cuda_check(cudaHostGetDevicePointer((void**)&st->d_stop, st->h_stop, 0), "stop flag");
+        cuda_check(cudaEventCreateWithFlags(&st->done, cudaEventDisableTiming), "event");
+        dev_chains ch{st->d_x, st->d_y, st->d_c, st->d_last};
+        unsigned ww = w, hh = h, sd = seed, salt = k->salt, wc = warmup_count;
+        unsigned long long* wh = st->d_counters + kCounterWords + 97;
+        void* args[] = {&st->d_samples, &ch, &ww, &hh, &sd, &salt, &wc, &wh};
+        launch(k->f_warmup, (unsigned)st->grid, (unsigned)k->block, s, args, "rfk_warmup");
+        cuda_check(cudaMemcpyAsync(&st->warmup_hits, wh, sizeof(unsigned long long), cudaMemcpyDeviceToHost, s), "D2H");
+        cuda_check(cudaStreamSynchronize(s), "warmup");
+        *out = st.release();
+    });
+}
+
+void rfk_state_destroy(rfk_state* s) { delete s; }
+
+rfk_status rfk_bin_async(rfk_state* st, const rfk_bailout* bo, void* stream) {
+    return guard([&] {
+        if (!st || !bo) fail(RFK_E_INVALID, "null argument");
+        if (!(bo->quality >= 0.0)) fail(RFK_E_INVALID, "quality must be >= 0");
+        if (bo->quality == 0.0 && bo->iters == 0 && bo->millis == 0)
+            fail(RFK_E_INVALID, "bailout needs a quality, pass or time limit");
+        const kernel_impl& k = *st->k;
+        cudaStream_t s = (cudaStream_t)stream;
+        cuda_check(rfk_launch_clear_counters(st->d_counters, s), "clear counters");
+        cuda_check(cudaMemsetAsync(st->d_counters + kCounterWords, 0, 98 * sizeof(unsigned long long), s), "clear histogram");
+        cuda_check(cudaMemsetAsync(st->d_stop, 0, sizeof(unsigned), s), "clear stop flag");
+        dev_bin_args a{};
+        a.samples = st->d_samples;
+        a.st = {st->d_x, st->d_y, st->d_c, st->d_last};
+        a.bins = st->d_bins;
+        a.w = st->w;
+        a.h = st->h;
+        a.seed = st->seed;
+        a.salt = k.salt;
+        a.call_id = st->call_id++ % 0xFFF0u;
+        const double pixels = (double)st->w * st->h;
+        a.quality_target = bo->quality > 0 ? (unsigned long long)(bo->quality * pixels * 255.0) : 0ull;
+        a.max_passes = bo->iters;
+        a.time_ns = (unsigned long long)bo->millis * 1000000ull;
+        a.stop = st->d_stop;
+        a.counters = st->d_counters;
+        void* args[] = {&a};
+        launch(k.f_bin, (unsigned)st->grid, (unsigned)k.block, s, args, "rfk_bin");
+        cuda_check(rfk_launch_density_histogram(st->d_bins, st->w * st->h, st->d_counters + kCounterWords,
+                                                st->d_counters + kCounterWords + 97, s),
+                   "density histogram");
+        cuda_check(cudaMemcpyAsync(st->h_counters, st->d_counters, (kCounterWords + 98) * sizeof(unsigned long long),
+                                   cudaMemcpyDeviceToHost, s),
+                   "D2H counters");
+        cuda_check(cudaEventRecord(st->done, s), "event");
+        st->pending = true;
+    });
+}
+
+rfk_status rfk_bin_wait(rfk_state* st, rfk_bin_result* out) {
+    return guard([&] {
+        if (!st) fail(RFK_E_INVALID, "null state");
+        if (!st->pending) fail(RFK_E_INVALID, "no bin call pending");
+        cuda_check(cudaEventSynchronize(st->done), "bin");
+        st->pending = false;
+        const unsigned long long* c = st->h_counters;
+        const double pixels = (double)st->w * st->h;
+        rfk_bin_result r{};
+        r.quality = (double)c[0] / (pixels * 255.0);
+        r.elapsed_ms = c[3] > c[2] ? (double)(c[3] - c[2]) / 1e6 : 0.0;
+        r.total_passes = c[1];
+        r.total_draws = c[0] / 255;
+        r.total_bins = (uint64_t)pixels;
+        r.passes_per_thread = (double)c[1] / ((double)st->grid * st->k->block);
+        r.max_density = (double)c[kCounterWords + 97];
+        r.draw_count = c[4];
+        r.status = (uint32_t)(c[5] & 0xFFFFFFFFu);
+        st->quality += r.quality;
+        if (out) *out = r;
+    });
+}
+
+rfk_status rfk_bin(rfk_state* st, const rfk_bailout* bo, void* stream, rfk_bin_result* out) {
+    rfk_status s = rfk_bin_async(st, bo, stream);
+    if (s != RFK_OK) return s;
+    return rfk_bin_wait(st, out);
+}
+
+rfk_status rfk_state_abort(rfk_state* st) {
+    return guard([&] {
+        if (!st || !st->h_stop) fail(RFK_E_INVALID, "null state");
+        *reinterpret_cast<volatile unsigned*>(st->h_stop) = 1u;
+    });
+}
+
+float* rfk_state_bins(rfk_state* st) { return st ? reinterpret_cast<float*>(st->d_bins) : nullptr; }
+
+double rfk_state_quality(const rfk_state* st) { return st ? st->quality : 0.0; }
+
+rfk_status rfk_state_chains(rfk_state* st, float* x, float* y, float* c, size_t cap, size_t* count) {
+    return guard([&] {
+        if (!st) fail(RFK_E_INVALID, "null state");
+        if (count) *count = st->nchains;
+        if (!x && !y && !c) return;
+        if (cap < st->nchains) fail(RFK_E_INVALID, "output buffers too small");
+        cuda_check(cudaDeviceSynchronize(), "sync");
+        if (x) cuda_check(cudaMemcpy(x, st->d_x, st->nchains * 4, cudaMemcpyDeviceToHost), "D2H");
+        if (y) cuda_check(cudaMemcpy(y, st->d_y, st->nchains * 4, cudaMemcpyDeviceToHost), "D2H");
+        if (c) cuda_check(cudaMemcpy(c, st->d_c, st->nchains * 4, cudaMemcpyDeviceToHost), "D2H");
+    });
+}
+
+rfk_status rfk_state_samples(rfk_state* st, float* out, size_t cap, size_t* count) {
+    return guard([&] {
+        if (!st) fail(RFK_E_INVALID, "null state");
+        const size_t n = (size_t)st->grid * st->k->sample_floats;
+        if (count) *count = n;
+        if (!out) return;
+        if (cap < n) fail(RFK_E_INVALID, "output buffer too small");
+        cuda_check(cudaDeviceSynchronize(), "sync");
+        cuda_check(cudaMemcpy(out, st->d_samples, n * 4, cudaMemcpyDeviceToHost), "D2H");
+    });
+}
+
+rfk_status rfk_apply_xform(const rfk_kernel* kh, const float* params, int xform, const float* in_xyc, size_t n,
+                           float* out_xyco, uint32_t seed) {
+    return guard([&] {
+        const kernel_impl& k = K(kh);
+        if (!params || !in_xyc || !out_xyco) fail(RFK_E_INVALID, "null argument");
+        if (xform >= (int)k.gen.num_xforms || xform < -1 || (xform == -1 && !k.gen.has_final))
+            fail(RFK_E_INVALID, "bad xform index");
+        if (n == 0) return;
+        if (n > (1u << 30)) fail(RFK_E_INVALID, "too many points");
+        float *dp = nullptr, *di = nullptr, *dout = nullptr;
+        cuda_check(cudaMalloc(&dp, k.sample_floats * 4), "alloc");
+        cuda_check(cudaMalloc(&di, n * 12), "alloc");
+        cuda_check(cudaMalloc(&dout, n * 16), "alloc");
+        cuda_check(cudaMemcpy(dp, params, k.sample_floats * 4, cudaMemcpyHostToDevice), "H2D");
+        cuda_check(cudaMemcpy(di, in_xyc, n * 12, cudaMemcpyHostToDevice), "H2D");
+        unsigned nn = (unsigned)n, sd = seed;
+        int xf = xform;
+        void* args[] = {&dp, &xf, &di, &dout, &nn, &sd};
+        launch(k.f_apply, (unsigned)((n + 255) / 256), 256, nullptr, args, "rfk_apply");
+        cuda_check(cudaMemcpy(out_xyco, dout, n * 16, cudaMemcpyDeviceToHost), "D2H");
+        cudaFree(dp);
+        cudaFree(di);
+        cudaFree(dout);
+    });
+}
+
+rfk_status rfk_prepare_samples(const rfk_kernel* kh, const double* samples, size_t nsamples, const uint32_t* seg,
+                               const float* t, size_t count, uint32_t seed, float* out) {
+    return guard([&] {
+        const kernel_impl& k = K(kh);
+        if (!samples || !seg || !t || !out) fail(RFK_E_INVALID, "null argument");
+        if (count == 0) return;
+        std::vector<unsigned> sg(seg, seg + count);
+        std::vector<float> tt(t, t + count);
+        float* d = nullptr;
+        cuda_check(cudaMalloc(&d, count * k.sample_floats * 4), "alloc");
+        prepare(k, samples, nsamples, sg, tt, seed, d, nullptr);
+        cuda_check(cudaMemcpy(out, d, count * k.sample_floats * 4, cudaMemcpyDeviceToHost), "D2H");
+        cudaFree(d);
+    });
+}
+
+rfk_status rfk_tonemap(const float* bins, uint32_t w, uint32_t h, void* out, int format, const rfk_tonemap_args* a,
+                       uint64_t* histogram, uint64_t* max_density, void* stream) {
+    return guard([&] {
+        if (!bins || !out || !a) fail(RFK_E_INVALID, "null argument");
+        if (format < RFK_HALF3 || format > RFK_FLOAT4) fail(RFK_E_INVALID, "bad output format");
+        if ((histogram == nullptr) != (max_density == nullptr)) fail(RFK_E_INVALID, "histogram and max_density go together");
+        if (!(a->quality > 0.0)) fail(RFK_E_INVALID, "quality must be positive");
+        if ((uint64_t)w * h > 0xFFFFFFFFull) fail(RFK_E_INVALID, "image too large");
+        // host constant as tonemapper.cpp:52, in single precision
+        const float scale_constant = std::pow(10.0f, -std::log10((float)a->quality) - 0.5f);
+        cuda_check(rfk_launch_tonemap(reinterpret_cast<const float4*>(bins), w * h, out, format, a->precise, (float)a->gamma,
+                                      scale_constant, (float)a->brightness, (float)a->vibrancy, (float)a->highlight_power,
+                                      (unsigned long long*)histogram, (unsigned long long*)max_density, (cudaStream_t)stream),
+                   "tonemap");
+    });
+}
+
+rfk_status rfk_density_histogram(const float* bins, uint32_t count, uint64_t* histogram, uint64_t* max_density,
+                                 void* stream) {
+    return guard([&] {
+        if (!bins || !histogram || !max_density) fail(RFK_E_INVALID, "null argument");
+        cuda_check(rfk_launch_density_histogram(reinterpret_cast<const float4*>(bins), count, (unsigned long long*)histogram,
+                                                (unsigned long long*)max_density, (cudaStream_t)stream),
+                   "density histogram");
+    });
+}
+
+rfk_status rfk_density_blur(const float* in, float* out, uint32_t w, uint32_t h, const rfk_de_args* a, void* stream) {
+    return guard([&] {
+        if (!in || !out || !a) fail(RFK_E_INVALID, "null argument");
+        if (in == out) fail(RFK_E_INVALID, "density blur needs distinct input and output");
+        if (!(a->max_radius >= 0.0) || a->max_radius > RFK_DE_MAX_RADIUS_CAP) fail(RFK_E_INVALID, "max_radius must be in [0, 9]");
+        if (!(a->min_radius >= 0.0) || a->min_radius > a->max_radius) fail(RFK_E_INVALID, "min_radius must be in [0, max_radius]");
+        if (!(a->curve >= 0.0)) fail(RFK_E_INVALID, "curve must be >= 0");
+        cuda_check(rfk_launch_de_blur(reinterpret_cast<const float4*>(in), reinterpret_cast<float4*>(out), w, h, (float)a->max_radius,
+                                      (float)a->min_radius, (float)a->curve, (cudaStream_t)stream),
+                   "density blur");
+    });
+}
+
+rfk_status rfk_catmull_coefficients(const double* samples, uint32_t sample_size, uint32_t nseg, float* coeff, void* stream) {
+    return guard([&] {
+        if (!samples || !coeff) fail(RFK_E_INVALID, "null argument");
+        cuda_check(rfk_launch_catmull(samples, sample_size, nseg, reinterpret_cast<float4*>(coeff), (cudaStream_t)stream), "catmull");
+    });
+}
+
+rfk_status rfk_fix_rotation(double* samples, size_t nsamples, size_t sample_size, size_t flame_size,
+                            const size_t* affine_indices, size_t n_affine) {
+    return guard([&] {
+        if (!samples || (!affine_indices && n_affine)) fail(RFK_E_INVALID, "null argument");
+        if (flame_size > sample_size) fail(RFK_E_INVALID, "flame_size > sample_size");
+        for (size_t i = 0; i < n_affine; i++)
+            if (affine_indices[i] + 6 > flame_size) fail(RFK_E_INVALID, "affine index out of range");
+        std::vector<double> v(samples, samples + nsamples * sample_size);
+        rfk::fix_rotation(v, sample_size, flame_size, std::vector<size_t>(affine_indices, affine_indices + n_affine));
+        std::copy(v.begin(), v.end(), samples);
+    });
+}
+
+rfk_status rfk_probe_red_v4(size_t bytes, uint32_t iters, double* ops_per_s) {
+    return guard([&] {
+        if (!ops_per_s || bytes < 16) fail(RFK_E_INVALID, "bad argument");
+        float4* buf = nullptr;
+        cuda_check(cudaMalloc(&buf, bytes), "alloc");
+        cuda_check(cudaMemset(buf, 0, bytes), "clear");
+        const unsigned blocks = (unsigned)device_sm_count() * 8, threads = 256;
+        cudaEvent_t a, b;
+        cudaEventCreate(&a);
+        cudaEventCreate(&b);
+        cuda_check(rfk_launch_red_v4_probe(buf, bytes / 16, iters, blocks, threads, nullptr), "probe");
+        cudaEventRecord(a);
+        cuda_check(rfk_launch_red_v4_probe(buf, bytes / 16, iters, blocks, threads, nullptr), "probe");
+        cudaEventRecord(b);
+        cuda_check(cudaEventSynchronize(b), "probe");
+        float ms = 0;
+        cudaEventElapsedTime(&ms, a, b);
+        cudaEventDestroy(a);
+        cudaEventDestroy(b);
+        cudaFree(buf);
+        *ops_per_s = (double)blocks * threads * iters / (ms * 1e-3);
+    });
+}
+
+int rfk_device_sm_count(void) {
+    int n = 0;
+    rfk_status s = guard([&] { n = device_sm_count(); });
+    return s == RFK_OK ? n : 0;
+}
+
+}  // extern "C"

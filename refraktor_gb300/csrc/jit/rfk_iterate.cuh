@@ -1,0 +1,473 @@
+// Chaos-game kernels, specialised per flame structure by NVRTC.
+//
+// The flame compiler prepends rfk_device.cuh and the generated flame code,
+// which defines:
+//   RFK_NX, RFK_HAS_FINAL, RFK_CHAOS, RFK_SIZE_REALS, RFK_NUM_AFFINES,
+//   rfk_affine_idx[], rfk_xf_base[] (offset of each xform's weight),
+//   R rfk_dispatch(int k, V2& p, R& c, const float* P, Rng& rng)   (standard xforms)
+//   R rfk_final(V2& p, R& c, const float* P, Rng& rng)              (if RFK_HAS_FINAL)
+//   void rfk_precalc(float* P, Rng& rng)                             (variation precalc)
+// and the launch shape: RFK_BLOCK (threads per block), RFK_CPT (chains per
+// thread), RFK_FLUSH (0 = one red.global.add.v4.f32 per draw, 1 = warp-
+// aggregated red for lanes that hit the same pixel), RFK_CHECK (passes
+// between bailout checks).
+//
+// Reference behaviour restated here (assets/kernels/refactor.cu):
+//   :99-117,:266-294  per temporal sample: flame = Catmull-Rom at t, affines
+//                     polar -> Cartesian, palette HSV -> 8-bit RGB (:128-147)
+//   :296-308          precalc, Hammersley start points mapped through the
+//                     plane-space affine, colour ~ U(0,1)
+//   :176-238          pass: pick xform, apply, bad-value reset
+//   :347-386          final xform on a copy, screen affine, trunc, bounds,
+//                     palette lerp between floor/ceil of colour*255, draw
+//   :404-475          persistent loop with quality / time / stop-flag bailout
+// Differences by design: each chain picks its own xform from a cumulative
+// weight table in shared memory (the reference votes one xform per warp and
+// shuffles iterators through the block); histogram updates are atomic
+// red.global.add.v4.f32 (the reference does a racy load/add/store); the RNG is
+// counter-based Philox keyed by (seed, flame salt) with counter (chain, sub,
+// pass).
+
+#ifndef RFK_BLOCK
+#define RFK_BLOCK 256
+#endif
+#ifndef RFK_CPT
+#define RFK_CPT 1
+#endif
+#ifndef RFK_FLUSH
+#define RFK_FLUSH 0
+#endif
+#ifndef RFK_CHECK
+#define RFK_CHECK 32
+#endif
+
+// Per-sample parameter block (floats).
+#define RFK_OFF_CUM (RFK_SIZE_REALS)
+#define RFK_OFF_FB (RFK_OFF_CUM + RFK_NX)
+#define RFK_OFF_CCUM (RFK_OFF_FB + 1)
+#define RFK_OFF_CFB (RFK_OFF_CCUM + (RFK_CHAOS ? RFK_NX * RFK_NX : 0))
+#define RFK_OFF_PAL_RAW (RFK_OFF_CFB + (RFK_CHAOS ? RFK_NX : 0))
+#define RFK_OFF_PAL (((RFK_OFF_PAL_RAW) + 3) / 4 * 4)
+#define RFK_SAMPLE_FLOATS (RFK_OFF_PAL + 1024)
+
+// Status bits reported to the host.
+#define RFK_ST_QUALITY 1u
+#define RFK_ST_TIME 2u
+#define RFK_ST_STOP 4u
+#define RFK_ST_ITERS 8u
+
+struct rfk_counters {
+    unsigned long long quality;   // sum of (u32)(255 * opacity) over draws
+    unsigned long long passes;    // chain steps
+    unsigned long long start_ns;  // earliest block start (%globaltimer)
+    unsigned long long stop_ns;   // latest block stop
+    unsigned long long draws;     // in-bounds draws with opacity > 0
+    unsigned int status;          // RFK_ST_* bits seen by any block
+    unsigned int pad;
+};
+
+__device__ __forceinline__ unsigned long long rfk_time() {
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
+__device__ __forceinline__ void rfk_red_v4(float4* addr, float a, float b, float c, float d) {
+    asm volatile("red.global.add.v4.f32 [%0], {%1, %2, %3, %4};" ::"l"(addr), "f"(a), "f"(b), "f"(c), "f"(d)
+                 : "memory");
+}
+
+// Chain state, structure of arrays over chains.
+struct rfk_chains {
+    float* x;
+    float* y;
+    float* c;
+    unsigned char* last;  // previous xform (chaos), 255 = none
+};
+
+// ---------------------------------------------------------------- prepare --
+// One block per temporal sample: evaluate the spline segment at t, convert
+// affines, build the palette, run precalc, build the xform pick tables.
+extern "C" __global__ void __launch_bounds__(256) rfk_prepare(const float4* __restrict__ coeff, unsigned sample_size,
+                                                              const unsigned* __restrict__ seg_of, const float* __restrict__ t_of,
+                                                              float* __restrict__ out, unsigned seed, unsigned salt) {
+    __shared__ float P[RFK_SAMPLE_FLOATS];
+    const unsigned s = blockIdx.x;
+    const float t = t_of[s];
+    const float4* seg = coeff + (size_t)seg_of[s] * sample_size;
+
+    for (unsigned i = threadIdx.x; i < RFK_SIZE_REALS; i += blockDim.x) {
+        float4 k = seg[i];  // a t^3 + b t^2 + c t + d
+        P[i] = fmaf(fmaf(fmaf(k.x, t, k.y), t, k.z), t, k.w);
+    }
+    for (unsigned i = threadIdx.x; i < 256; i += blockDim.x) {
+        float hsv[3];
+        for (int j = 0; j < 3; j++) {
+            float4 k = seg[RFK_SIZE_REALS + 3 * i + j];
+            hsv[j] = fmaf(fmaf(fmaf(k.x, t, k.y), t, k.z), t, k.w);
+        }
+        // HSV -> RGB as refactor.cu:128-140, truncated to 8 bits
+        float rgb[3];
+        const float ns[3] = {5.0f, 3.0f, 1.0f};
+        for (int j = 0; j < 3; j++) {
+            float kk = fmodf(ns[j] + hsv[0] / 60.0f, 6.0f);
+            float f = hsv[2] - hsv[2] * hsv[1] * fmaxf(0.0f, fminf(kk, fminf(4.0f - kk, 1.0f)));
+            float v = f * 255.0f;
+            rgb[j] = (float)(unsigned char)fminf(fmaxf(v, 0.0f), 255.0f) / 255.0f;
+        }
+        P[RFK_OFF_PAL + 4 * i + 0] = rgb[0];
+        P[RFK_OFF_PAL + 4 * i + 1] = rgb[1];
+        P[RFK_OFF_PAL + 4 * i + 2] = rgb[2];
+        P[RFK_OFF_PAL + 4 * i + 3] = 0.0f;
+    }
+    __syncthreads();
+    if (threadIdx.x < RFK_NUM_AFFINES) {
+        const unsigned a = rfk_affine_idx[threadIdx.x];
+        const float angx = P[a], angy = P[a + 1];
+        const float magx = expf(P[a + 2]), magy = expf(P[a + 3]);
+        float sx, cx, sy, cy;
+        sincosf(angx, &sx, &cx);
+        sincosf(angy, &sy, &cy);
+        P[a] = magx * cx;
+        P[a + 1] = magx * sx;
+        P[a + 2] = magy * cy;
+        P[a + 3] = magy * sy;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        Rng rng;
+        rng.start(s, 0xFFFFu, 0xFFFFFFFFFFFFFFFFull, seed, salt);
+        // weight sum and pick table (flame.tpl:110-123 semantics)
+        float wsum = 0.0f;
+        for (int i = 0; i < RFK_NX; i++) wsum += P[rfk_xf_base[i]];
+        P[12] = wsum;
+        float run = 0.0f;
+        int last_nonzero = 0;
+        for (int i = 0; i < RFK_NX; i++) {
+            float w = P[rfk_xf_base[i]];
+            run += w;
+            P[RFK_OFF_CUM + i] = (w != 0.0f) ? run : -1.0f;
+            if (w != 0.0f) last_nonzero = i;
+        }
+        P[RFK_OFF_FB] = __int_as_float(last_nonzero);
+#if RFK_CHAOS
+        // chaos rows (flame.tpl:170-177): weights[j] *= xform_j.weight
+        for (int r = 0; r < RFK_NX; r++) {
+            const unsigned row = 13 + r * (RFK_NX + 1);
+            float rs = 0.0f;
+            for (int j = 0; j < RFK_NX; j++) {
+                P[row + 1 + j] *= P[rfk_xf_base[j]];
+                rs += P[row + 1 + j];
+            }
+            P[row] = rs;
+            float rr = 0.0f;
+            int ln = 0;
+            for (int j = 0; j < RFK_NX; j++) {
+                float w = P[row + 1 + j];
+                rr += w;
+                P[RFK_OFF_CCUM + r * RFK_NX + j] = (w != 0.0f) ? rr : -1.0f;
+                if (w != 0.0f) ln = j;
+            }
+            P[RFK_OFF_CFB + r] = __int_as_float(ln);
+        }
+#endif
+        // screen jitter ~ gauss(1/3 px) for antialiasing (flame.tpl:179-182)
+        V2 j = rng.gauss(1.0f / 3.0f);
+        P[4] += j.x;
+        P[5] += j.y;
+        rfk_precalc(P, rng);
+    }
+    __syncthreads();
+    float* dst = out + (size_t)s * RFK_SAMPLE_FLOATS;
+    for (unsigned i = threadIdx.x; i < RFK_SAMPLE_FLOATS; i += blockDim.x) dst[i] = P[i];
+}
+
+// ------------------------------------------------------------- chain step --
+__device__ __forceinline__ int rfk_pick(float u, const float* __restrict__ P, unsigned last) {
+#if RFK_CHAOS
+    if (last != 255u) {
+        const float ratio = u * P[13 + last * (RFK_NX + 1)];
+        const float* cum = P + RFK_OFF_CCUM + last * RFK_NX;
+        int k = __float_as_int(P[RFK_OFF_CFB + last]);
+#pragma unroll
+        for (int i = RFK_NX - 2; i >= 0; i--)
+            if (cum[i] >= ratio) k = i;
+        return k;
+    }
+#endif
+    const float ratio = u * P[12];
+    int k = __float_as_int(P[RFK_OFF_FB]);
+#pragma unroll
+    for (int i = RFK_NX - 2; i >= 0; i--)
+        if (P[RFK_OFF_CUM + i] >= ratio) k = i;
+    return k;
+}
+
+// One chaos-game step of one chain. Returns the draw (pixel index or -1) and
+// its RGBA contribution.
+__device__ __forceinline__ int rfk_step(float& x, float& y, float& c, unsigned& last, Rng& rng,
+                                        const float* __restrict__ P, unsigned w, unsigned h, float4& contrib,
+                                        unsigned& hit) {
+    const int k = rfk_pick(rng.u01(), P, last);
+#if RFK_CHAOS
+    last = (unsigned)k;
+#endif
+    V2 p = fl_vec2(x, y);
+    R col = c;
+    R op = rfk_dispatch(k, p, col, P, rng);
+    if (rfk_badvalue(p.x) || rfk_badvalue(p.y)) {
+        p.x = rng.u01() * 2.0f - 1.0f;
+        p.y = rng.u01() * 2.0f - 1.0f;
+        op = 0.0f;
+    }
+    x = p.x;
+    y = p.y;
+    c = col;
+#if RFK_HAS_FINAL
+    rfk_final(p, col, P, rng);
+#endif
+    // screen-space affine (a,d,b,e,c,f at P[0..5])
+    float sx = fmaf(P[0], p.x, fmaf(P[2], p.y, P[4]));
+    float sy = fmaf(P[1], p.x, fmaf(P[3], p.y, P[5]));
+    sx = truncf(sx);
+    sy = truncf(sy);
+    hit = 0;
+    if (sx >= 0.0f && sy >= 0.0f && sx < (float)w && sy < (float)h && op > 0.0f) {
+        const float pi = fminf(fmaxf(col, 0.0f), 1.0f) * 255.0f;
+        const float lo_f = floorf(pi);
+        const int lo = (int)lo_f, hi = (int)ceilf(pi);
+        const float mix = pi - lo_f;
+        const float4* pal = reinterpret_cast<const float4*>(P + RFK_OFF_PAL);
+        const float4 a = pal[lo], b = pal[hi];
+        contrib.x = ((1.0f - mix) * a.x + mix * b.x) * op;
+        contrib.y = ((1.0f - mix) * a.y + mix * b.y) * op;
+        contrib.z = ((1.0f - mix) * a.z + mix * b.z) * op;
+        contrib.w = op;
+        hit = (unsigned)(255.0f * op);
+        return (int)sy * (int)w + (int)sx;
+    }
+    return -1;
+}
+
+__device__ __forceinline__ void rfk_flush(float4* __restrict__ bins, int idx, float4 v) {
+#if RFK_FLUSH == 1
+    // lanes that hit the same pixel add their contributions first
+    const unsigned active = __activemask();
+    const unsigned same = __match_any_sync(active, idx);
+    if (idx >= 0) {
+        const int leader = __ffs(same) - 1;
+        const unsigned lane = threadIdx.x & 31u;
+        unsigned rest = same & ~(1u << leader);
+        float4 acc = v;
+        while (rest) {
+            const int src = __ffs(rest) - 1;
+            rest &= rest - 1;
+            float4 o;
+            o.x = __shfl_sync(same, v.x, src);
+            o.y = __shfl_sync(same, v.y, src);
+            o.z = __shfl_sync(same, v.z, src);
+            o.w = __shfl_sync(same, v.w, src);
+            acc.x += o.x; acc.y += o.y; acc.z += o.z; acc.w += o.w;
+        }
+        if ((int)lane == leader) rfk_red_v4(bins + idx, acc.x, acc.y, acc.z, acc.w);
+    }
+#else
+    if (idx >= 0) rfk_red_v4(bins + idx, v.x, v.y, v.z, v.w);
+#endif
+}
+
+// --------------------------------------------------------------- warmup ----
+// Hammersley point idx of `total` (refactor.cu:10-54), in [-1, 1]^2.
+__device__ __forceinline__ V2 rfk_hammersley(unsigned idx, unsigned total) {
+    unsigned max_val = (total % 2u == 0u) ? total : (1u << (32 - __clz(total - 1u)));
+    unsigned radix = 31u - __clz(max_val);
+    float inv = 1.0f / (float)max_val;
+    unsigned flipped = (radix == 0u) ? 0u : (__brev(idx) >> (32u - radix));
+    return fl_vec2((float)idx * inv * 2.0f - 1.0f, (float)flipped * inv * 2.0f - 1.0f);
+}
+
+// Chain j of block b is chain index (k * gridDim.x + b) * RFK_BLOCK + tid for
+// k in [0, RFK_CPT). Each block owns one temporal sample (sample = block).
+extern "C" __global__ void __launch_bounds__(RFK_BLOCK) rfk_warmup(const float* __restrict__ samples, rfk_chains st,
+                                                                   unsigned w, unsigned h, unsigned seed, unsigned salt,
+                                                                   unsigned warmup_count,
+                                                                   unsigned long long* __restrict__ warmup_hits) {
+    __shared__ __align__(16) float P[RFK_SAMPLE_FLOATS];
+    __shared__ unsigned long long block_hits;
+    const float* src = samples + (size_t)blockIdx.x * RFK_SAMPLE_FLOATS;
+    for (unsigned i = threadIdx.x; i < RFK_SAMPLE_FLOATS; i += RFK_BLOCK) P[i] = src[i];
+    if (threadIdx.x == 0) block_hits = 0;
+    __syncthreads();
+    const unsigned total = gridDim.x * RFK_BLOCK * RFK_CPT;
+    unsigned long long my_hits = 0;
+#pragma unroll 1
+    for (int k = 0; k < RFK_CPT; k++) {
+        const unsigned chain = (k * gridDim.x + blockIdx.x) * RFK_BLOCK + threadIdx.x;
+        Rng rng;
+        rng.start(chain, 0xFFFDu, 0ull, seed, salt);
+        V2 pos = rfk_hammersley(chain, total);
+        float px = (pos.x + 1.0f) / 2.0f * (float)w;
+        float py = (pos.y + 1.0f) / 2.0f * (float)h;
+        // plane-space affine at P[6..11]
+        float x = fmaf(P[6], px, fmaf(P[8], py, P[10]));
+        float y = fmaf(P[7], px, fmaf(P[9], py, P[11]));
+        float c = rng.u01();
+        unsigned last = 255u;
+#pragma unroll 1
+        for (unsigned pass = 0; pass < warmup_count; pass++) {
+            Rng r2;
+            r2.start(chain, 0xFFFEu, (unsigned long long)pass, seed, salt);
+            float4 contrib;
+            unsigned hit;
+            rfk_step(x, y, c, last, r2, P, w, h, contrib, hit);
+            my_hits += hit;
+        }
+        st.x[chain] = x;
+        st.y[chain] = y;
+        st.c[chain] = c;
+#if RFK_CHAOS
+        st.last[chain] = (unsigned char)last;
+#endif
+    }
+    atomicAdd(&block_hits, my_hits);
+    __syncthreads();
+    if (threadIdx.x == 0) atomicAdd(warmup_hits, block_hits);
+}
+
+// ------------------------------------------------------------------ bin ----
+struct rfk_bin_args {
+    const float* samples;
+    rfk_chains st;
+    float4* bins;
+    unsigned w, h;
+    unsigned seed, salt;
+    unsigned call_id, pad0;             // call_id selects this call's Philox sub-stream
+    unsigned long long quality_target;  // stop when counters->quality >= this (0 = no target)
+    unsigned long long max_passes;      // per-chain cap for this call (0 = no cap)
+    unsigned long long time_ns;         // time budget per block (0 = none)
+    const volatile unsigned* stop;      // host-written stop flag (may be null)
+    rfk_counters* counters;
+};
+
+extern "C" __global__ void __launch_bounds__(RFK_BLOCK) rfk_bin(rfk_bin_args a) {
+    __shared__ __align__(16) float P[RFK_SAMPLE_FLOATS];
+    __shared__ unsigned long long s_hits, s_draws;
+    __shared__ unsigned s_bail;
+    __shared__ unsigned long long s_start;
+    const float* src = a.samples + (size_t)blockIdx.x * RFK_SAMPLE_FLOATS;
+    for (unsigned i = threadIdx.x; i < RFK_SAMPLE_FLOATS; i += RFK_BLOCK) P[i] = src[i];
+    if (threadIdx.x == 0) {
+        s_hits = 0;
+        s_draws = 0;
+        s_bail = 0;
+        s_start = rfk_time();
+        atomicMin(&a.counters->start_ns, s_start);
+    }
+    float x[RFK_CPT], y[RFK_CPT], c[RFK_CPT];
+    unsigned last[RFK_CPT];
+    unsigned chain[RFK_CPT];
+#pragma unroll
+    for (int k = 0; k < RFK_CPT; k++) {
+        chain[k] = (k * gridDim.x + blockIdx.x) * RFK_BLOCK + threadIdx.x;
+        x[k] = a.st.x[chain[k]];
+        y[k] = a.st.y[chain[k]];
+        c[k] = a.st.c[chain[k]];
+#if RFK_CHAOS
+        last[k] = a.st.last[chain[k]];
+#else
+        last[k] = 255u;
+#endif
+    }
+    __syncthreads();
+
+    unsigned long long pass = 0;
+    unsigned my_hits = 0, my_draws = 0;
+#pragma unroll 1
+    for (;;) {
+#pragma unroll 1
+        for (int it = 0; it < RFK_CHECK; it++) {
+#pragma unroll
+            for (int k = 0; k < RFK_CPT; k++) {
+                Rng rng;
+                rng.start(chain[k], a.call_id, pass, a.seed, a.salt);
+                float4 v;
+                unsigned hit;
+                int idx = rfk_step(x[k], y[k], c[k], last[k], rng, P, a.w, a.h, v, hit);
+                rfk_flush(a.bins, idx, v);
+                my_hits += hit;
+                my_draws += (idx >= 0) ? 1u : 0u;
+            }
+            pass++;
+        }
+        // bailout check: block totals -> global counters -> decision
+        unsigned wh = __reduce_add_sync(0xffffffffu, my_hits);
+        unsigned wd = __reduce_add_sync(0xffffffffu, my_draws);
+        my_hits = 0;
+        my_draws = 0;
+        if ((threadIdx.x & 31u) == 0) {
+            atomicAdd(&s_hits, (unsigned long long)wh);
+            atomicAdd(&s_draws, (unsigned long long)wd);
+        }
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            unsigned long long q = atomicAdd(&a.counters->quality, s_hits) + s_hits;
+            atomicAdd(&a.counters->draws, s_draws);
+            s_hits = 0;
+            s_draws = 0;
+            unsigned bail = 0;
+            if (a.quality_target && q >= a.quality_target) bail |= RFK_ST_QUALITY;
+            if (a.max_passes && pass >= a.max_passes) bail |= RFK_ST_ITERS;
+            if (a.time_ns && rfk_time() - s_start >= a.time_ns) bail |= RFK_ST_TIME;
+            if (a.stop && *a.stop) bail |= RFK_ST_STOP;
+            if (!bail && a.quality_target) {
+                // another block may have met the target already
+                unsigned long long gq = *((volatile unsigned long long*)&a.counters->quality);
+                if (gq >= a.quality_target) bail |= RFK_ST_QUALITY;
+            }
+            s_bail = bail;
+        }
+        __syncthreads();
+        if (s_bail) break;
+    }
+#pragma unroll
+    for (int k = 0; k < RFK_CPT; k++) {
+        a.st.x[chain[k]] = x[k];
+        a.st.y[chain[k]] = y[k];
+        a.st.c[chain[k]] = c[k];
+#if RFK_CHAOS
+        a.st.last[chain[k]] = (unsigned char)last[k];
+#endif
+    }
+    if (threadIdx.x == 0) {
+        atomicAdd(&a.counters->passes, pass * (unsigned long long)(RFK_BLOCK * RFK_CPT));
+        atomicOr(&a.counters->status, s_bail);
+        atomicMax(&a.counters->stop_ns, rfk_time());
+    }
+}
+
+// ------------------------------------------------------ single application --
+// Applies one xform (or the final xform, xform < 0) of one prepared parameter
+// block to n points (x, y, colour): the single-map unit of the parity tests.
+// Random draws come from Philox stream (point index, sub 0xFFFC).
+extern "C" __global__ void __launch_bounds__(256) rfk_apply(const float* __restrict__ params, int xform,
+                                                            const float* __restrict__ in, float* __restrict__ out,
+                                                            unsigned n, unsigned seed) {
+    const unsigned i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    Rng rng;
+    rng.start(i, 0xFFFCu, 0ull, seed, 0u);
+    V2 p = fl_vec2(in[3 * i], in[3 * i + 1]);
+    R c = in[3 * i + 2];
+    R op = 0.0f;
+    if (xform < 0) {
+#if RFK_HAS_FINAL
+        op = rfk_final(p, c, params, rng);
+#endif
+    } else {
+        op = rfk_dispatch(xform, p, c, params, rng);
+    }
+    out[4 * i] = p.x;
+    out[4 * i + 1] = p.y;
+    out[4 * i + 2] = c;
+    out[4 * i + 3] = op;
+}

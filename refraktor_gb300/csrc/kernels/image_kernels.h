@@ -1,0 +1,29 @@
+// Launchers of the flame-independent kernels (image.cu).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#define RFK_HISTOGRAM_BINS 97  // granularity 4: 24 * 4 + 1 log2 bins (constants.h:4-6 of the reference)
+#define RFK_DE_STEPS 4         // blur radius quantisation: 1/4 px
+#define RFK_DE_MAX_RADIUS_CAP 9
+#define RFK_DE_LEVELS (RFK_DE_MAX_RADIUS_CAP * RFK_DE_STEPS + 1)
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+cudaError_t rfk_launch_catmull(const double* samples, unsigned sample_size, unsigned nseg, float4* coeff, cudaStream_t s);
+cudaError_t rfk_launch_tonemap(const float4* bins, unsigned size, void* out, int format, int precise, float gamma,
+                               float scale_constant, float brightness, float vibrancy, float highlight_power,
+                               unsigned long long* hist, unsigned long long* max_density, cudaStream_t s);
+cudaError_t rfk_launch_density_histogram(const float4* bins, unsigned size, unsigned long long* hist,
+                                         unsigned long long* max_density, cudaStream_t s);
+cudaError_t rfk_launch_de_blur(const float4* in, float4* out, unsigned w, unsigned h, float max_radius, float min_radius,
+                               float curve, cudaStream_t s);
+cudaError_t rfk_launch_red_v4_probe(float4* buf, unsigned long long n, unsigned iters, unsigned blocks, unsigned threads,
+                                    cudaStream_t s);
+cudaError_t rfk_launch_clear_counters(unsigned long long* c, cudaStream_t s);
+
+#ifdef __cplusplus
+}
+#endif

@@ -1,0 +1,129 @@
+"""Seeded synthetic genomes for the benchmark workloads.
+
+The reference publishes no benchmark genomes, so the workloads are generated:
+  plain_flame(seed)          512x512, 3 xforms (weights 0.5/0.3/0.2), variations
+                             from {linear, sinusoidal, spherical}
+  hd_flame(seed)             1920x1080, 8 xforms with Dirichlet(1) weights plus a
+                             final xform, 1-3 variations each from the 14-set
+Affine 2x2 parts are uniform in [-1, 1] rescaled to spectral norm <= 0.9,
+translations uniform in [-1, 1]; variation weights U[0, 1]; colour per xform
+U[0, 1]; colour speed 0.5; opacity 1; the palette is an HSV cubic spline
+through 8 seeded knots. The default camera is centre (0, 0), scale 0.25
+(the image height spans 4 units); frame_on_gpu() refits centre and scale to
+the 1% / 99% quantiles of the chain positions after a GPU warm-up.
+Genomes are emitted in the reference JSON layout (flame_types.cpp:399-485)
+with the palette as [h, s, v] triples.
+"""
+from __future__ import annotations
+
+import math
+
+import numpy as np
+
+PLAIN_SET = ["linear", "sinusoidal", "spherical"]
+HD_SET = ["linear", "sinusoidal", "spherical", "swirl", "horseshoe", "polar", "handkerchief", "heart", "disc", "spiral",
+          "hyperbolic", "julia", "exponential", "power"]
+
+
+def _affine(rng: np.random.Generator) -> list[float]:
+    m = rng.uniform(-1.0, 1.0, size=(2, 2))
+    n = np.linalg.norm(m, 2)
+    if n > 0.9:
+        m *= 0.9 / n
+    c, f = rng.uniform(-1.0, 1.0, size=2)
+    # reference order a, d, b, e, c, f for [[a b c], [d e f]]
+    return [float(m[0, 0]), float(m[1, 0]), float(m[0, 1]), float(m[1, 1]), float(c), float(f)]
+
+
+def palette(rng: np.random.Generator) -> list[list[float]]:
+    """256 HSV entries from a periodic cubic spline through 8 seeded knots."""
+    knots = rng.uniform(0.0, 1.0, size=(8, 3))
+    knots[:, 0] *= 360.0
+    knots[:, 1] = 0.4 + 0.6 * knots[:, 1]
+    knots[:, 2] = 0.5 + 0.5 * knots[:, 2]
+    out = []
+    for i in range(256):
+        u = i / 256.0 * 8.0
+        k = int(math.floor(u))
+        t = u - k
+        p = [knots[(k + j - 1) % 8] for j in range(4)]
+        # Catmull-Rom through the knots (uniform)
+        v = 0.5 * ((2 * p[1]) + (-p[0] + p[2]) * t + (2 * p[0] - 5 * p[1] + 4 * p[2] - p[3]) * t * t +
+                   (-p[0] + 3 * p[1] - 3 * p[2] + p[3]) * t ** 3)
+        h = float(v[0] % 360.0)
+        out.append([h, float(np.clip(v[1], 0.0, 1.0)), float(np.clip(v[2], 0.0, 1.0))])
+    return out
+
+
+def _xform(rng: np.random.Generator, weight: float, names: list[str]) -> dict:
+    return {
+        "weight": float(weight),
+        "color": float(rng.uniform(0.0, 1.0)),
+        "color_speed": 0.5,
+        "opacity": 1.0,
+        "vchain": [{
+            "transform": _affine(rng),
+            "mod_x": 0.0, "mod_y": 0.0, "mod_scale": 1.0, "mod_rotate": 0.0,
+            "variations": {n: float(rng.uniform(0.0, 1.0)) for n in sorted(set(names))},
+        }],
+    }
+
+
+def frame_on_gpu(db, genome: dict, w: int, h: int, seed: int = 0) -> dict:
+    """Refits centre and scale so that the 1%..99% box of the attractor fills
+    the image, from the chain positions after a warm-up on the GPU."""
+    from . import librefrakt as lr
+
+    f = lr.flame.from_json(db, genome)
+    k = lr.flame_compiler().get_flame_kernel(db, f)
+    st = k.warmup(f.pack_samples(4, w, h), (w, h), seed, 64)
+    xy = st.chains()[:2].T
+    xy = xy[np.all(np.isfinite(xy), axis=1)]
+    out = dict(genome)
+    if xy.shape[0] < 16:
+        return out
+    lo = np.quantile(xy, 0.01, axis=0)
+    hi = np.quantile(xy, 0.99, axis=0)
+    cx, cy = (lo + hi) / 2.0
+    span_x, span_y = max(hi[0] - lo[0], 1e-3), max(hi[1] - lo[1], 1e-3)
+    # screen = (p - centre) * scale * h + (w/2, h/2): fit both extents, 5% margin
+    out["center_x"], out["center_y"] = float(cx), float(cy)
+    out["scale"] = float(min(w / (span_x * h), 1.0 / span_y) * 0.95)
+    return out
+
+
+def _base(rng: np.random.Generator, gamma: float, brightness: float) -> dict:
+    return {
+        "center_x": 0.0, "center_y": 0.0, "scale": 0.25, "rotate": 0.0,
+        "gamma": gamma, "brightness": brightness, "vibrancy": 1.0, "highlight_power": -1.0, "gamma_threshold": 0.01,
+        "mod_hue": 0.0, "mod_sat": 0.0, "mod_val": 0.0,
+        "xforms": [],
+    }
+
+
+def plain_flame(seed: int = 0) -> dict:
+    rng = np.random.default_rng(seed)
+    g = _base(rng, 2.2, 4.0)
+    for wt in (0.5, 0.3, 0.2):
+        k = int(rng.integers(1, 4))
+        names = list(rng.choice(PLAIN_SET, size=k, replace=False))
+        g["xforms"].append(_xform(rng, wt, names))
+    g["palette"] = palette(rng)
+    return g
+
+
+def hd_flame(seed: int = 0, n_xforms: int = 8, final: bool = True, var_set: list[str] | None = None) -> dict:
+    rng = np.random.default_rng(seed + 1_000_003)
+    g = _base(rng, 2.2, 4.0)
+    weights = rng.dirichlet(np.ones(n_xforms))
+    for wt in weights:
+        k = int(rng.integers(1, 4))
+        names = list(rng.choice(var_set or HD_SET, size=k, replace=False))
+        g["xforms"].append(_xform(rng, wt, names))
+    if final:
+        k = int(rng.integers(1, 4))
+        names = list(rng.choice(var_set or HD_SET, size=k, replace=False))
+        fx = _xform(rng, 0.0, names)
+        g["final_xform"] = fx
+    g["palette"] = palette(rng)
+    return g

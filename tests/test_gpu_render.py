@@ -1,0 +1,220 @@
+"""GPU parity of the chaos game: interpolation, single map application,
+converged renders against the FP64 oracle, and the bailout / resume / abort
+behaviour of warmup + bin."""
+import threading
+import time
+
+import numpy as np
+import pytest
+
+torch = pytest.importorskip("torch")
+
+from oracle import oracle as orc
+from refraktor_gb300 import librefrakt as lr
+from refraktor_gb300 import synthetic as syn
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def comp():
+    return lr.flame_compiler()
+
+
+def _one_variation_flame(name, seed):
+    rng = np.random.default_rng(seed)
+    g = syn.plain_flame(seed)
+    m = rng.uniform(-1, 1, size=(2, 2))
+    g["xforms"] = [{"weight": 1.0, "color": 0.3, "color_speed": 0.5, "opacity": 1.0,
+                    "vchain": [{"transform": [m[0, 0], m[1, 0], m[0, 1], m[1, 1], *rng.uniform(-0.5, 0.5, 2)],
+                                "mod_x": 0, "mod_y": 0, "mod_scale": 1, "mod_rotate": 0,
+                                "variations": {name: float(rng.uniform(0.2, 1.0))}}]}]
+    return g
+
+
+def test_warmup_and_bin_reach_quality(db, comp):
+    g = syn.plain_flame(0)
+    f = lr.flame.from_json(db, g)
+    k = comp.get_flame_kernel(db, f)
+    w, h = 256, 192
+    st = k.warmup(f.pack_samples(4, w, h), (w, h), seed=1, count=20)
+    r = k.bin(st, lr.bailout_args(iters=0, millis=0, quality=8.0))
+    assert r.status & 1
+    assert 8.0 <= r.quality < 8.0 * 1.2
+    assert r.total_bins == w * h
+    bins = st.bins().cpu().numpy()
+    # opacity 1 everywhere: density sum = draws = quality * pixels
+    assert abs(bins[..., 3].sum() - r.draw_count) <= 1e-4 * r.draw_count
+    assert r.total_draws == int(r.quality * w * h)
+    assert r.max_density == pytest.approx(float(np.floor(bins[..., 3].max())), abs=1.0)
+    # resume: a second call keeps accumulating
+    r2 = k.bin(st, lr.bailout_args(iters=0, millis=0, quality=4.0))
+    assert st.quality == pytest.approx(r.quality + r2.quality)
+    bins2 = st.bins().cpu().numpy()
+    assert bins2[..., 3].sum() > bins[..., 3].sum() * 1.4
+
+
+def test_pass_cap_and_time_bailouts(db, comp):
+    f = lr.flame.from_json(db, syn.plain_flame(1))
+    k = comp.get_flame_kernel(db, f)
+    st = k.warmup(f.pack_samples(4, 64, 64), (64, 64), seed=2, count=10)
+    r = k.bin(st, lr.bailout_args(iters=64, millis=0, quality=0))
+    assert r.status == 8
+    chains = k.info["grid"] * k.info["block"] * k.info["chains_per_thread"]
+    assert r.total_passes == 64 * chains
+    t0 = time.time()
+    r = k.bin(st, lr.bailout_args(iters=0, millis=50, quality=0))
+    assert r.status & 2
+    assert 40 <= r.elapsed_ms < 2000
+    assert time.time() - t0 < 5
+
+
+def test_abort_from_another_thread(db, comp):
+    f = lr.flame.from_json(db, syn.plain_flame(2))
+    k = comp.get_flame_kernel(db, f)
+    st = k.warmup(f.pack_samples(4, 64, 64), (64, 64), seed=3, count=10)
+    k.bin_async(st, lr.bailout_args(iters=0, millis=20000, quality=0))
+    threading.Timer(0.2, st.abort_binning).start()
+    t0 = time.time()
+    r = st.wait()
+    assert r.status & 4
+    assert time.time() - t0 < 10
+
+
+def test_deterministic_with_pass_cap(db, comp):
+    g = syn.plain_flame(4)
+    f = lr.flame.from_json(db, g)
+    k = comp.get_flame_kernel(db, f)
+    outs = []
+    for _ in range(2):
+        st = k.warmup(f.pack_samples(4, 96, 96), (96, 96), seed=9, count=20)
+        k.bin(st, lr.bailout_args(iters=40, millis=0, quality=0))
+        outs.append(st.bins().cpu().numpy())
+    # atomics reorder float sums; the counts (alpha) are exact
+    np.testing.assert_array_equal(outs[0][..., 3], outs[1][..., 3])
+    np.testing.assert_allclose(outs[0], outs[1], rtol=1e-5, atol=1e-6)
+
+
+def test_prepared_flame_matches_oracle_interpolation(db, comp):
+    """Row a3/a4: FP32 Catmull-Rom + polar affines + 8-bit palette vs FP64."""
+    rng = np.random.default_rng(11)
+    g = syn.hd_flame(3)
+    f = lr.flame.from_json(db, g)
+    k = comp.get_flame_kernel(db, f)
+    w, h = 640, 360
+    base = f.pack_sample(w, h)
+    R = f.size_reals()
+    keys = []
+    for i in range(5):
+        s = base.copy()
+        s[13:R] += rng.normal(0, 0.05, R - 13)
+        s[R:] = base[R:]
+        keys.append(s)
+    samples = np.concatenate(keys)
+    seg = np.array([0, 0, 1, 1, 0, 1], dtype=np.uint32)
+    t = np.array([0.0, 0.3, 0.5, 0.99, 0.75, 0.1], dtype=np.float32)
+    got = k.prepare_samples(samples, seg, t)
+    aff = set()
+    for a in f.affine_indices():
+        aff.update(range(a, a + 4))
+    for i in range(len(seg)):
+        p_ref, pal_ref = orc.prepared(g, w, h, t=float(t[i]), seg=int(seg[i]), samples=samples)
+        p = got[i, :R].astype(np.float64)
+        # weight sum slot, jitter-shifted screen translation and precalc slots are device-computed
+        mask = np.ones(R, bool)
+        mask[[4, 5, 12]] = False
+        scale = np.max(np.abs(samples.reshape(5, -1)[seg[i]:seg[i] + 4, :R]), axis=0)
+        tol = 4 * np.spacing(scale.astype(np.float32)).astype(np.float64)
+        for j in aff:  # exp / cos of interpolated angles and log magnitudes
+            tol[j] = 8 * np.spacing(np.float32(max(abs(p_ref[j]), 1e-3)))
+        assert np.all((np.abs(p - p_ref) <= tol)[mask]), np.nonzero((np.abs(p - p_ref) > tol) & mask)
+        # screen translation moved by the Gaussian(1/3 px) jitter
+        assert abs(p[4] - p_ref[4]) < 3.0 and abs(p[5] - p_ref[5]) < 3.0
+        pal = got[i, k.info["sample_floats"] - 1024:].reshape(256, 4)[:, :3]
+        assert np.all(np.abs(pal - pal_ref) <= 1.0 / 255 + 1e-6)
+        assert np.mean(np.abs(pal - pal_ref) < 1e-6) > 0.98
+
+
+DETERMINISTIC = ["linear", "sinusoidal", "spherical", "swirl", "horseshoe", "polar", "handkerchief", "heart", "disc",
+                 "spiral", "hyperbolic", "exponential", "power", "fisheye", "bubble", "diamond", "ex", "bent",
+                 "cylinder", "exp", "eyefish", "cosine"]
+
+
+def _ulp_errors(got, ref):
+    """Error in FP32 ulps of the larger output component of each point."""
+    scale = np.maximum(np.abs(ref[:, 0]), np.abs(ref[:, 1]))
+    ulp = np.spacing(np.maximum(scale, 1e-30).astype(np.float32)).astype(np.float64)
+    return np.max(np.abs(got[:, :2] - ref[:, :2]), axis=1) / ulp
+
+
+@pytest.mark.parametrize("name", DETERMINISTIC)
+def test_single_map_within_4_ulp(db, comp, name):
+    """One map application (affine + variation) in the precise-math build vs
+    an FP64 evaluation of the same formula on the same FP32 inputs: at least
+    99% of points within 4 ulp, every point within 64 ulp (cancellation)."""
+    g = _one_variation_flame(name, seed=hash(name) % 1000)
+    f = lr.flame.from_json(db, g)
+    k = comp.get_flame_kernel(db, f, precise_math=1)
+    prep = k.prepare_samples(f.pack_samples(4, 256, 256), [0], [0.0])[0]
+    rng = np.random.default_rng(12)
+    n = 4096
+    pts = np.stack([rng.uniform(-1.5, 1.5, n), rng.uniform(-1.5, 1.5, n), rng.uniform(0, 1, n)], 1).astype(np.float32)
+    out = k.apply_xform(prep, 0, pts).astype(np.float64)
+    P = prep[:f.size_reals()].astype(np.float64)
+    ref = np.array([orc.apply(g, P, 0, float(x), float(y), float(c))[:4] for x, y, c in pts])
+    ok = np.isfinite(ref[:, 0]) & np.isfinite(ref[:, 1]) & (np.abs(ref[:, :2]).max(axis=1) < 1e6)
+    e = _ulp_errors(out[ok], ref[ok])
+    assert np.mean(e <= 4) >= 0.99, (name, np.percentile(e, [50, 99, 100]))
+    assert np.all(e <= 64), (name, float(e.max()))
+    np.testing.assert_allclose(out[:, 2], ref[:, 2], rtol=1e-6, atol=1e-7)  # colour blend
+    assert np.all(out[:, 3] == 1.0)
+
+
+def _density(hist):
+    d = hist[..., 3].astype(np.float64)
+    return d / d.sum()
+
+
+def test_render_matches_oracle_below_noise_floor(db, comp):
+    """Converged-render parity: normalised density L1 between the GPU and the
+    FP64 oracle at equal spp is within 1.25x the L1 between two oracle seeds,
+    and both shrink as spp grows (no bias floor)."""
+    g = syn.plain_flame(0)
+    w = h = 128
+    f = lr.flame.from_json(db, g)
+    k = comp.get_flame_kernel(db, f)
+    res = {}
+    for spp in (16.0, 256.0):
+        st = k.warmup(f.pack_samples(4, w, h), (w, h), seed=5, count=20)
+        k.bin(st, lr.bailout_args(iters=0, millis=0, quality=spp))
+        gpu = _density(st.bins().cpu().numpy())
+        chains = 16384
+        passes = int(spp * w * h / chains) + 1
+        o1, _ = orc.render(g, w, h, chains, passes, seed=1, threads=8)
+        o2, _ = orc.render(g, w, h, chains, passes, seed=2, threads=8)
+        floor = np.abs(_density(o1) - _density(o2)).sum()
+        d_gpu = np.abs(gpu - _density(o1)).sum()
+        res[spp] = (d_gpu, floor)
+        assert d_gpu < 1.25 * floor, (spp, d_gpu, floor)
+    assert res[256.0][0] < 0.5 * res[16.0][0]
+
+
+def test_hd_render_colour_matches_oracle(db, comp):
+    """8 xforms + final xform, 14-variation set: density and colour channels."""
+    g = syn.hd_flame(0)
+    w, h = 160, 90
+    f = lr.flame.from_json(db, g)
+    k = comp.get_flame_kernel(db, f)
+    st = k.warmup(f.pack_samples(4, w, h), (w, h), seed=6, count=20)
+    r = k.bin(st, lr.bailout_args(iters=0, millis=0, quality=64.0))
+    gpu = st.bins().cpu().numpy().astype(np.float64)
+    chains = 16384
+    passes = int(64.0 * w * h / chains / max(r.draw_count / max(r.total_passes, 1), 0.05)) + 1
+    o1, _ = orc.render(g, w, h, chains, passes, seed=3, threads=8)
+    o2, _ = orc.render(g, w, h, chains, passes, seed=4, threads=8)
+    for c in range(4):
+        a = gpu[..., c] / gpu[..., c].sum()
+        b = o1[..., c] / o1[..., c].sum()
+        b2 = o2[..., c] / o2[..., c].sum()
+        floor = np.abs(b - b2).sum()
+        assert np.abs(a - b).sum() < 1.25 * floor + 0.01, (c, np.abs(a - b).sum(), floor)
