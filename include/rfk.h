@@ -134,7 +134,7 @@ void rfk_state_destroy(rfk_state* s);
 /* flame_kernel::bailout_args  flame_compiler.h:92-96 */
 typedef struct {
     uint32_t iters;   /* passes per chain cap for this call (0 = none) */
-    uint32_t millis;  /* time budget (0 = none) */
+    uint32_t millis;  /* time budget; 0 or above 60000 means 60000 (every call ends) */
     double quality;   /* additional spp to reach (0 = none) */
 } rfk_bailout;
 

@@ -107,6 +107,7 @@ struct dev_bin_args {
     unsigned long long* counters;
 };
 constexpr int kCounterWords = 6;  // quality, passes, start, stop, draws, status|pad
+constexpr uint32_t kMaxBinMillis = 60000;  // upper bound of one bin call
 
 }  // namespace
 
@@ -616,7 +617,10 @@ rfk_status rfk_bin_async(rfk_state* st, const rfk_bailout* bo, void* stream) {
         const double pixels = (double)st->w * st->h;
         a.quality_target = bo->quality > 0 ? (unsigned long long)(bo->quality * pixels * 255.0) : 0ull;
         a.max_passes = bo->iters;
-        a.time_ns = (unsigned long long)bo->millis * 1000000ull;
+        // Every call carries a time budget so that a target the flame can never
+        // reach (all draws off-screen) still ends: min(millis, kMaxBinMillis).
+        const uint32_t ms = (bo->millis == 0 || bo->millis > kMaxBinMillis) ? kMaxBinMillis : bo->millis;
+        a.time_ns = (unsigned long long)ms * 1000000ull;
         a.stop = st->d_stop;
         a.counters = st->d_counters;
         void* args[] = {&a};

@@ -121,8 +121,8 @@ extern "C" __global__ void __launch_bounds__(256) rfk_prepare(const float4* __re
         P[RFK_OFF_PAL + 4 * i + 3] = 0.0f;
     }
     __syncthreads();
-    if (threadIdx.x < RFK_NUM_AFFINES) {
-        const unsigned a = rfk_affine_idx[threadIdx.x];
+    for (unsigned ai = threadIdx.x; ai < RFK_NUM_AFFINES; ai += blockDim.x) {
+        const unsigned a = rfk_affine_idx[ai];
         const float angx = P[a], angy = P[a + 1];
         const float magx = expf(P[a + 2]), magy = expf(P[a + 3]);
         float sx, cx, sy, cy;
