@@ -1,0 +1,310 @@
+"""Benchmark of the flame-rendering hot path (see the design doc for the contract).
+
+Workload: the plain 1080p single flame - 1920x1080, 1024 spp, 8 xforms with
+Dirichlet(1) weights plus a final xform, 1-3 variations each from the
+14-variation set, density-estimation blur (radius 0-9 px ~ 1/sqrt(density)),
+tonemap; seeded synthetic genome (synthetic.hd_flame(0), camera fitted on the
+GPU), since the reference publishes no benchmark genomes.
+
+One step = one frame: bin to 1024 spp on a warmed state (value), or the full
+public-API path from host genome samples to a host image (e2e).
+  value  iterations/s (chain steps per second), device-timed with CUDA events
+         around the bin calls on their stream, histogram already resident
+  e2e    the same metric through rfk_warmup + rfk_bin + rfk_density_blur +
+         rfk_tonemap with host samples in and the host image out
+Between timed steps a 512 MiB buffer is written to flush L2 (129 MB).
+
+--impl reference times the reference path on the CPU: the reference has no
+CPU implementation, so this is the FP64 oracle port (oracle/), on all host
+cores, over a bounded sample of the same workload.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+W, H, SPP = 1920, 1080, 1024.0
+WARMUP_PASSES = 20
+METRIC = "iterations/s"
+WORKLOAD = "plain 1080p single flame: 1920x1080, 1024 spp, 8 xforms + final xform, 14-variation set, DE blur, tonemap"
+
+
+def _dist():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    return ws, rank
+
+
+class ClockSampler:
+    """nvidia-smi samples of SM clock and throttle reasons during the timed region."""
+
+    def __init__(self, gpu: int = 0):
+        self.gpu = gpu
+        self.rows: list[list[str]] = []
+        self._stop = threading.Event()
+        self._proc = None
+
+    def __enter__(self):
+        q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+             "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+             "clocks_event_reasons.sw_power_cap")
+        try:
+            self._proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={q}", "--format=csv,noheader,nounits",
+                                           "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            threading.Thread(target=self._read, daemon=True).start()
+        except FileNotFoundError:
+            self._proc = None
+        return self
+
+    def _read(self):
+        for line in self._proc.stdout:
+            self.rows.append([c.strip() for c in line.split(",")])
+
+    def __exit__(self, *exc):
+        if self._proc:
+            self._proc.terminate()
+            try:
+                self._proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self._proc.kill()
+
+    def summary(self) -> dict:
+        rows = [r for r in self.rows if len(r) >= 7]
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm = [float(r[0]) for r in rows if r[0].replace(".", "").isdigit()]
+        reasons = set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in rows:
+            for n, v in zip(names, r[3:7]):
+                if v.strip().lower() == "active":
+                    reasons.add(n)
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": float(rows[0][1]) if rows else None,
+                "reasons": sorted(reasons), "samples": len(rows)}
+
+
+def _flush_l2(buf):
+    buf.fill_(1.0)
+
+
+def run_gpu(args) -> dict:
+    import torch
+
+    from refraktor_gb300 import build
+    from refraktor_gb300 import librefrakt as lr
+    from refraktor_gb300 import synthetic as syn
+
+    ws, rank = _dist()
+    torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+    if ws > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl")
+    build.build()
+    db = lr.flamedb()
+    genome = syn.frame_on_gpu(db, syn.hd_flame(0), W, H)
+    f = lr.flame.from_json(db, genome)
+    tp = f.tonemap_params()
+    comp = lr.flame_compiler()
+    k = comp.get_flame_kernel(db, f)
+    samples = f.pack_samples(4, W, H)
+    stream = torch.cuda.Stream()
+    flush = torch.empty(512 << 20 >> 2, dtype=torch.float32, device="cuda")
+
+    # ---- value: bin to 1024 spp on a warmed state, device-timed ------------
+    st = k.warmup(samples, (W, H), seed=rank + 1, count=WARMUP_PASSES, stream=stream)
+    bo = lr.bailout_args(iters=0, millis=0, quality=SPP)
+    for _ in range(args.warmup):
+        k.bin(st, bo, stream=stream)
+    times, passes, draws, elapsed_kernel = [], 0, 0, 0.0
+    with ClockSampler(int(os.environ.get("LOCAL_RANK", "0"))) as clocks:
+        for _ in range(args.steps):
+            _flush_l2(flush)
+            torch.cuda.synchronize()
+            if ws > 1:
+                torch.distributed.barrier()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            k.bin_async(st, bo, stream=stream)
+            e1.record(stream)
+            r = st.wait()
+            torch.cuda.synchronize()
+            times.append(e0.elapsed_time(e1) / 1e3)
+            passes += r.total_passes
+            draws += r.draw_count
+            elapsed_kernel += r.elapsed_ms / 1e3
+    t_total = sum(times)
+    if ws > 1:
+        t = torch.tensor([t_total], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        t_total = float(t.item())
+        pt = torch.tensor([passes, draws], device="cuda", dtype=torch.float64)
+        torch.distributed.all_reduce(pt)
+        passes, draws = int(pt[0].item()), int(pt[1].item())
+    value = passes / t_total
+    bin_launch_s = t_total / args.steps
+
+    # roofline: draws are red.global.add.v4.f32 (16 B payload) into the L2-resident histogram
+    peak_ops = lr.probe_red_v4(W * H * 16, 512)
+    achieved_ops = draws / max(elapsed_kernel, 1e-9) if ws == 1 else draws / t_total
+    info = k.info
+
+    # ---- e2e: public API, host samples in, host image out ------------------
+    out_host = torch.empty((H, W, 4), dtype=torch.float16, pin_memory=True)
+    e2e_times = []
+    e2e_passes = 0
+    for i in range(args.warmup + args.steps):
+        _flush_l2(flush)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        s2 = k.warmup(samples, (W, H), seed=100 + i, count=WARMUP_PASSES, stream=stream)
+        r = k.bin(s2, bo, stream=stream)
+        blurred = torch.empty((H, W, 4), dtype=torch.float32, device="cuda")
+        with torch.cuda.stream(stream):
+            lr.density_blur(s2.bins(), blurred, (W, H), 9.0, 0.0, 0.5, stream=stream)
+            img = torch.empty((H, W, 4), dtype=torch.float16, device="cuda")
+            lr.tonemapper().run(blurred, img, (W, H), s2.quality, tp["gamma"], tp["brightness"], tp["vibrancy"],
+                                fmt=lr.HALF4, stream=stream)
+            out_host.copy_(img, non_blocking=True)
+        stream.synchronize()
+        dt = time.perf_counter() - t0
+        del s2
+        if i >= args.warmup:
+            e2e_times.append(dt)
+            e2e_passes += r.total_passes + k.info["grid"] * k.info["block"] * WARMUP_PASSES
+    e2e_t = sum(e2e_times)
+    if ws > 1:
+        t = torch.tensor([e2e_t], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        e2e_t = float(t.item())
+        pt = torch.tensor([e2e_passes], device="cuda", dtype=torch.float64)
+        torch.distributed.all_reduce(pt)
+        e2e_passes = int(pt.item())
+
+    line = {
+        "metric": METRIC,
+        "value": value,
+        "unit": "iterations/s",
+        "n_gpus": ws,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": 1e3 * t_total / args.steps,
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f32",
+        "data": "synthetic (seeded genome synthetic.hd_flame(0), camera fitted on the GPU)",
+        "config": {"workload": WORKLOAD, "width": W, "height": H, "spp": SPP, "xforms": 8, "final_xform": True,
+                   "grid": info["grid"], "block": info["block"], "chains_per_thread": info["chains_per_thread"],
+                   "flush": info["flush"], "l2": "512 MiB buffer written between timed steps",
+                   "parallelism": f"replicas x{ws}"},
+        "e2e": {"value": e2e_passes / e2e_t, "unit": "iterations/s", "s_per_frame": e2e_t / args.steps,
+                "h2d_bytes_per_step": int(samples.nbytes), "d2h_bytes_per_step": int(W * H * 4 * 2)},
+        "roofline": {"bound": "l2_atomic", "achieved": achieved_ops * 16 / 1e9, "peak": peak_ops * 16 / 1e9,
+                     "unit": "GB/s", "frac": achieved_ops / peak_ops, "traffic": None,
+                     "achieved_ops": achieved_ops, "peak_ops": peak_ops,
+                     "note": "red.global.add.v4.f32 payload (16 B per draw); peak = measured random red.v4 rate into a "
+                             "buffer of the histogram's size"},
+        "gpu_launches": args.steps * 3,
+        "clocks": clocks.summary(),
+        "draws_per_s": draws / t_total,
+        "bin_ms": 1e3 * bin_launch_s,
+        "registers": info["registers"],
+    }
+    if rank == 0 and not args.no_cpu_baseline:
+        line["cpu_baseline"] = cpu_baseline(genome, seconds=args.cpu_seconds)
+    if ws > 1:
+        torch.distributed.destroy_process_group()
+    return line if rank == 0 else {}
+
+
+def cpu_baseline(genome: dict, seconds: float = 12.0, threads: int | None = None) -> dict:
+    """The FP64 oracle chaos game on the host cores, bounded sample of the workload."""
+    from oracle import oracle as orc
+
+    threads = threads or os.cpu_count() or 1
+    chains = 64 * threads
+    params, pal = orc.prepared(genome, W, H)
+    # calibrate passes for about `seconds` of work
+    t0 = time.perf_counter()
+    orc.render(genome, W, H, chains, 200, warmup=WARMUP_PASSES, threads=threads, params=params, palette=pal)
+    dt = time.perf_counter() - t0
+    passes = max(200, int(200 * seconds / max(dt, 1e-3)))
+    t0 = time.perf_counter()
+    _, draws = orc.render(genome, W, H, chains, passes, warmup=WARMUP_PASSES, threads=threads, params=params,
+                          palette=pal)
+    dt = time.perf_counter() - t0
+    iters = chains * (passes + WARMUP_PASSES)
+    return {"value": iters / dt, "unit": "iterations/s", "cores": threads, "kind": "port",
+            "sample": f"{chains} chains x {passes + WARMUP_PASSES} passes of the same 1920x1080 flame "
+                      f"({iters / 1e9:.2f} G iterations, {draws / 1e9:.2f} G draws, {dt:.1f} s)",
+            "draws_per_s": draws / dt, "seconds": dt, "iterations": iters}
+
+
+def run_reference(args) -> dict:
+    """CPU reference leg: the FP64 oracle port on all host cores."""
+    ws, rank = _dist()
+    if rank != 0:
+        return {}
+    from refraktor_gb300 import synthetic as syn
+
+    genome = syn.hd_flame(0)
+    genome.update(center_x=0.0, center_y=0.0, scale=0.25)
+    try:
+        import torch  # noqa: F401
+
+        if torch.cuda.is_available():
+            from refraktor_gb300 import build
+            from refraktor_gb300 import librefrakt as lr
+
+            build.build()
+            genome = syn.frame_on_gpu(lr.flamedb(), syn.hd_flame(0), W, H)
+    except Exception:
+        pass
+    vals = []
+    for _ in range(args.warmup):
+        cpu_baseline(genome, seconds=2.0)
+    for _ in range(args.steps):
+        vals.append(cpu_baseline(genome, seconds=args.cpu_seconds / max(args.steps, 1)))
+    total_s = sum(x["seconds"] for x in vals)
+    v = sum(x["iterations"] for x in vals) / total_s
+    return {
+        "metric": METRIC, "value": v, "unit": "iterations/s", "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": 1e3 * total_s / max(args.steps, 1),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic (seeded genome synthetic.hd_flame(0))",
+        "config": {"workload": WORKLOAD, "width": W, "height": H, "spp": SPP},
+        "impl": "reference",
+        "cpu_baseline": {"value": v, "unit": "iterations/s", "cores": vals[0]["cores"], "kind": "port",
+                         "sample": vals[0]["sample"]},
+        "e2e": {"value": v, "unit": "iterations/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--cpu-seconds", type=float, default=12.0)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    line = run_reference(args) if args.impl == "reference" else run_gpu(args)
+    if line:
+        print(json.dumps(line))
+
+
+if __name__ == "__main__":
+    main()

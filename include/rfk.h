@@ -87,7 +87,6 @@ typedef struct {
     int chains_per_thread; /* 0 = 1 */
     int flush;             /* histogram update: 0 = red.global.add.v4.f32 per draw, 1 = warp-aggregated */
     int blocks_per_sm;     /* 0 = as many as fit */
-    int check_interval;    /* passes between bailout checks (0 = 32) */
 } rfk_compile_opts;
 
 typedef struct {
@@ -223,8 +222,10 @@ rfk_status rfk_density_blur(const float* bins_in, float* bins_out, uint32_t w, u
                             void* stream);
 
 /* generate_sample_coefficients  assets/kernels/catmull.cu:33-42: device FP64
- * samples [nseg + 3][sample_size] -> device FP32 coefficients
- * [nseg][sample_size][4] (a, b, c, d of a t^3 + b t^2 + c t + d). */
+ * samples [nseg + 3][sample_size] -> device FP32 segments
+ * [nseg][sample_size][4] in Hermite form (p1, p2, m1, m2): the curve is
+ * h00(t) p1 + h01(t) p2 + h10(t) m1 + h11(t) m2, the same cubic as the
+ * reference's a t^3 + b t^2 + c t + d with m1, m2 its centripetal tangents. */
 rfk_status rfk_catmull_coefficients(const double* samples, uint32_t sample_size, uint32_t nseg, float* coeff,
                                     void* stream);
 

@@ -371,7 +371,7 @@ static void* render_job(void* arg) {
 
 uint64_t oracle_render(const int* structure, const double* params, const double* pal, uint32_t w, uint32_t h,
                        uint64_t n_chains, uint32_t warmup, uint64_t passes, uint64_t seed, int threads, int n_jitter,
-                       double* hist) {
+                       const double* jitter_in, double* hist) {
     flame_desc* d = (flame_desc*)malloc(sizeof(flame_desc));
     if (!d || parse_structure(structure, d) < 0 || d->chaos) {
         free(d);
@@ -384,6 +384,11 @@ uint64_t oracle_render(const int* structure, const double* params, const double*
     rng_t jr;
     rng_seed(&jr, seed ^ 0xA5A5A5A5A5A5ull);
     for (int i = 0; i < n_jitter; i++) {
+        if (jitter_in) {
+            jit[2 * i] = jitter_in[2 * i];
+            jit[2 * i + 1] = jitter_in[2 * i + 1];
+            continue;
+        }
         const double a = u01(&jr) * 2.0;
         const double r = (1.0 / 3.0) * (u01(&jr) + u01(&jr) + u01(&jr) + u01(&jr) - 2.0);
         jit[2 * i] = r * cos(PI * a);
@@ -451,7 +456,8 @@ void oracle_tonemap(const float* bins, size_t n, double quality, double gamma, d
             o[0] = o[1] = o[2] = o[3] = 0.0;
             continue;
         }
-        const double f = 0.5 * B * log10(1.0 + w_in * (double)k2) / w_in;
+        /* log10(1 + x) evaluated as log1p(x) / ln 10 so that tiny densities keep their digits */
+        const double f = 0.5 * B * (log1p(w_in * (double)k2) / log(10.0)) / w_in;
         double c[3] = {bins[4 * i] * f, bins[4 * i + 1] * f, bins[4 * i + 2] * f};
         const double wf = w_in * f;
         const double gf = pow(wf, inv_gamma) / wf;

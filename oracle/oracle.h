@@ -68,12 +68,13 @@ double oracle_apply(const int* structure, const double* params, int xf, double* 
 /* FP64 chaos game (refactor.cu:176-238, :347-386 semantics with per-chain
  * xform picks): n_chains chains, `warmup` passes without drawing, then
  * `passes` drawing passes, into hist [h][w][4] (doubles, summed). The screen
- * affine of each chain gets one of `n_jitter` Gaussian(1/3 px) offsets
+ * affine of chain i gets offset i % n_jitter of `jitter` (n_jitter x 2), or
+ * when `jitter` is NULL, of n_jitter Gaussian(1/3 px) offsets it draws
  * (flame.tpl:179-182). Runs on `threads` POSIX threads. Returns the number
  * of draws. */
 uint64_t oracle_render(const int* structure, const double* params, const double* palette_rgb, uint32_t w, uint32_t h,
                        uint64_t n_chains, uint32_t warmup, uint64_t passes, uint64_t seed, int threads, int n_jitter,
-                       double* hist);
+                       const double* jitter, double* hist);
 
 /* tonemap (tonemap.cu:67-104, tonemapper.cpp:52) in FP64: bins [n][4] ->
  * out [n][4] (alpha in the 4th channel). highlight_power < 0 = off. */

@@ -48,7 +48,7 @@ def lib() -> C.CDLL:
                                    C.POINTER(C.c_double), C.c_void_p, C.POINTER(C.c_int)]
         L.oracle_apply.restype = C.c_double
         L.oracle_render.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_uint32, C.c_uint32, C.c_uint64, C.c_uint32,
-                                    C.c_uint64, C.c_uint64, C.c_int, C.c_int, C.c_void_p]
+                                    C.c_uint64, C.c_uint64, C.c_int, C.c_int, C.c_void_p, C.c_void_p]
         L.oracle_render.restype = C.c_uint64
         L.oracle_tonemap.argtypes = [C.c_void_p, C.c_size_t, C.c_double, C.c_double, C.c_double, C.c_double, C.c_double,
                                      C.c_void_p]
@@ -219,16 +219,39 @@ def apply(g: dict, params: np.ndarray, xf: int, x: float, y: float, c: float, u=
 
 
 def render(g: dict, w: int, h: int, chains: int, passes: int, warmup: int = 20, seed: int = 1, threads: int = 1,
-           n_jitter: int = 1024, params=None, palette=None) -> tuple[np.ndarray, int]:
+           n_jitter: int = 1024, params=None, palette=None, jitter=None) -> tuple[np.ndarray, int]:
+    """FP64 chaos game. `jitter` (n x 2) gives the screen offsets to cycle
+    over the chains; by default n_jitter Gaussian(1/3 px) offsets are drawn."""
     if params is None:
         params, palette = prepared(g, w, h)
     s = structure(g)
     hist = np.zeros((h, w, 4))
     P = np.ascontiguousarray(params, dtype=np.float64)
     pal = np.ascontiguousarray(palette, dtype=np.float64)
+    jp = None
+    if jitter is not None:
+        j = np.ascontiguousarray(jitter, dtype=np.float64).reshape(-1, 2)
+        n_jitter = j.shape[0]
+        jp = j.ctypes.data
     draws = lib().oracle_render(s.ctypes.data, P.ctypes.data, pal.ctypes.data, w, h, chains, warmup, passes, seed, threads,
-                                n_jitter, hist.ctypes.data)
+                                n_jitter, jp, hist.ctypes.data)
     return hist, int(draws)
+
+
+def hermite_eval(seg4: np.ndarray, t: float) -> np.ndarray:
+    """Evaluates (p1, p2, m1, m2) Hermite segments at t in FP64."""
+    s = np.asarray(seg4, dtype=np.float64)
+    h01 = t * t * (3 - 2 * t)
+    h00 = 1 - h01
+    h10 = t * (1 - t) ** 2
+    h11 = t * t * (t - 1)
+    return h00 * s[..., 0] + h01 * s[..., 1] + h10 * s[..., 2] + h11 * s[..., 3]
+
+
+def cubic_eval(coeff: np.ndarray, t: float) -> np.ndarray:
+    """Evaluates (a, b, c, d) segments (catmull.cu layout) at t in FP64."""
+    c = np.asarray(coeff, dtype=np.float64)
+    return ((c[..., 0] * t + c[..., 1]) * t + c[..., 2]) * t + c[..., 3]
 
 
 def tonemap(bins: np.ndarray, quality: float, gamma: float, brightness: float, vibrancy: float,

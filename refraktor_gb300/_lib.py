@@ -15,7 +15,7 @@ c_size_p = C.POINTER(C.c_size_t)
 
 class CompileOpts(C.Structure):
     _fields_ = [("precise_math", C.c_int), ("block", C.c_int), ("chains_per_thread", C.c_int), ("flush", C.c_int),
-                ("blocks_per_sm", C.c_int), ("check_interval", C.c_int)]
+                ("blocks_per_sm", C.c_int)]
 
 
 class KernelInfo(C.Structure):

@@ -99,7 +99,8 @@ struct dev_bin_args {
     float4* bins;
     unsigned w, h;
     unsigned seed, salt;
-    unsigned call_id, pad0;
+    unsigned call_id;
+    unsigned check;
     unsigned long long quality_target;
     unsigned long long max_passes;
     unsigned long long time_ns;
@@ -126,7 +127,7 @@ struct kernel_impl {
     std::string log;
     cudaLibrary_t lib = nullptr;
     cudaKernel_t f_prepare = nullptr, f_warmup = nullptr, f_bin = nullptr, f_apply = nullptr;
-    int block = 256, cpt = 1, flush = 0, grid = 0, regs = 0, check = 32;
+    int block = 256, cpt = 1, flush = 0, grid = 0, regs = 0;
     size_t sample_floats = 0;
     double compile_ms = 0.0;
     double sfu_per_iter = 0.0;
@@ -185,14 +186,13 @@ std::string full_source(const rfk::generated_flame& g) {
 }
 
 std::vector<char> nvrtc_build(const std::string& source, const std::string& arch_name, const rfk_compile_opts& o, int block,
-                              int cpt, int flush, int check, std::string& log) {
+                              int cpt, int flush, std::string& log) {
     const std::string arch = "--gpu-architecture=" + arch_name;
     const std::string d_block = "-DRFK_BLOCK=" + std::to_string(block);
     const std::string d_cpt = "-DRFK_CPT=" + std::to_string(cpt);
     const std::string d_flush = "-DRFK_FLUSH=" + std::to_string(flush);
-    const std::string d_check = "-DRFK_CHECK=" + std::to_string(check);
     std::vector<const char*> opts = {arch.c_str(), "-std=c++17", "-lineinfo", d_block.c_str(), d_cpt.c_str(),
-                                     d_flush.c_str(), d_check.c_str(), "-extra-device-vectorization"};
+                                     d_flush.c_str(), "-extra-device-vectorization"};
     if (!o.precise_math) opts.push_back("--use_fast_math");
     nvrtcProgram prog;
     if (nvrtcCreateProgram(&prog, source.c_str(), "rfk_flame.cu", 0, nullptr, nullptr) != NVRTC_SUCCESS)
@@ -221,7 +221,7 @@ void check_options(const rfk_compile_opts& o) {
     if (block % 32 != 0 || block > 1024) fail(RFK_E_INVALID, "block must be a multiple of 32 up to 1024");
     if (o.chains_per_thread > 8 || o.chains_per_thread < 0) fail(RFK_E_INVALID, "chains_per_thread must be in [0, 8]");
     if (o.flush < 0 || o.flush > 1) fail(RFK_E_INVALID, "flush must be 0 or 1");
-    if (o.check_interval < 0 || o.blocks_per_sm < 0) fail(RFK_E_INVALID, "negative option");
+    if (o.blocks_per_sm < 0) fail(RFK_E_INVALID, "negative option");
 }
 
 // NVRTC module cache: (db hash, structure, options) -> kernel.
@@ -235,7 +235,6 @@ std::shared_ptr<kernel_impl> compile(const rfk::flamedb& db, const rfk::flame& f
     k->block = o.block > 0 ? o.block : 256;
     k->cpt = o.chains_per_thread > 0 ? o.chains_per_thread : 1;
     k->flush = o.flush;
-    k->check = o.check_interval > 0 ? o.check_interval : 32;
     check_options(o);
     k->sample_floats = sample_floats_for(k->gen);
     if (k->sample_floats * 4 > 44 * 1024) fail(RFK_E_INVALID, "flame too large for the shared-memory parameter block");
@@ -243,7 +242,7 @@ std::shared_ptr<kernel_impl> compile(const rfk::flamedb& db, const rfk::flame& f
 
     k->source = full_source(k->gen);
 
-    std::vector<char> cubin = nvrtc_build(k->source, device_arch(), o, k->block, k->cpt, k->flush, k->check, log);
+    std::vector<char> cubin = nvrtc_build(k->source, device_arch(), o, k->block, k->cpt, k->flush, log);
     cuda_check(cudaLibraryLoadData(&k->lib, cubin.data(), nullptr, nullptr, 0, nullptr, nullptr, 0), "cudaLibraryLoadData");
     cuda_check(cudaLibraryGetKernel(&k->f_prepare, k->lib, "rfk_prepare"), "rfk_prepare");
     cuda_check(cudaLibraryGetKernel(&k->f_warmup, k->lib, "rfk_warmup"), "rfk_warmup");
@@ -275,7 +274,7 @@ std::shared_ptr<kernel_impl> compile_cached(const rfk::flamedb& db, const rfk::f
                                            std::string& log) {
     std::ostringstream key;
     key << db.hash() << "|" << f.structure_key() << "|" << o.precise_math << "," << o.block << "," << o.chains_per_thread
-        << "," << o.flush << "," << o.blocks_per_sm << "," << o.check_interval;
+        << "," << o.flush << "," << o.blocks_per_sm;
     {
         std::lock_guard<std::mutex> lk(g_cache_mu);
         auto it = g_cache.find(key.str());
@@ -517,7 +516,7 @@ rfk_status rfk_compile_check(const rfk_db* db, const rfk_flame* f, const rfk_com
         check_options(o);
         auto g = rfk::generate_flame_code(db->db, f->f);
         nvrtc_build(full_source(g), arch, o, o.block > 0 ? o.block : 256, o.chains_per_thread > 0 ? o.chains_per_thread : 1,
-                    o.flush, o.check_interval > 0 ? o.check_interval : 32, nlog);
+                    o.flush, nlog);
     });
     if (log && log_cap) copy_out(log, log_cap, nullptr, st == RFK_OK ? nlog : g_error);
     return st;
@@ -617,6 +616,13 @@ rfk_status rfk_bin_async(rfk_state* st, const rfk_bailout* bo, void* stream) {
         const double pixels = (double)st->w * st->h;
         a.quality_target = bo->quality > 0 ? (unsigned long long)(bo->quality * pixels * 255.0) : 0ull;
         a.max_passes = bo->iters;
+        // Passes between bailout checks: about 1/8 of the target per round of
+        // all chains, so the overshoot stays near one round when the target is
+        // small next to the chain count.
+        const double chains = (double)st->nchains;
+        double chk = a.quality_target ? (double)a.quality_target / (chains * 255.0 * 8.0) : 32.0;
+        chk = std::min(32.0, std::max(1.0, std::floor(chk)));
+        a.check = (unsigned)chk;
         // Every call carries a time budget so that a target the flame can never
         // reach (all draws off-screen) still ends: min(millis, kMaxBinMillis).
         const uint32_t ms = (bo->millis == 0 || bo->millis > kMaxBinMillis) ? kMaxBinMillis : bo->millis;

@@ -9,8 +9,7 @@
 //   void rfk_precalc(float* P, Rng& rng)                             (variation precalc)
 // and the launch shape: RFK_BLOCK (threads per block), RFK_CPT (chains per
 // thread), RFK_FLUSH (0 = one red.global.add.v4.f32 per draw, 1 = warp-
-// aggregated red for lanes that hit the same pixel), RFK_CHECK (passes
-// between bailout checks).
+// aggregated red for lanes that hit the same pixel).
 //
 // Reference behaviour restated here (assets/kernels/refactor.cu):
 //   :99-117,:266-294  per temporal sample: flame = Catmull-Rom at t, affines
@@ -36,9 +35,6 @@
 #endif
 #ifndef RFK_FLUSH
 #define RFK_FLUSH 0
-#endif
-#ifndef RFK_CHECK
-#define RFK_CHECK 32
 #endif
 
 // Per-sample parameter block (floats).
@@ -96,15 +92,21 @@ extern "C" __global__ void __launch_bounds__(256) rfk_prepare(const float4* __re
     const float t = t_of[s];
     const float4* seg = coeff + (size_t)seg_of[s] * sample_size;
 
+    // Hermite basis of the segment p1 -> p2 with tangents m1, m2 (the same
+    // cubic as a t^3 + b t^2 + c t + d of catmull.cu, evaluated so that t = 0
+    // and t = 1 return the knots exactly)
+    const float t2 = t * t;
+    const float h01 = t2 * (3.0f - 2.0f * t), h00 = 1.0f - h01;
+    const float h10 = t * (1.0f - t) * (1.0f - t), h11 = t2 * (t - 1.0f);
     for (unsigned i = threadIdx.x; i < RFK_SIZE_REALS; i += blockDim.x) {
-        float4 k = seg[i];  // a t^3 + b t^2 + c t + d
-        P[i] = fmaf(fmaf(fmaf(k.x, t, k.y), t, k.z), t, k.w);
+        const float4 k = seg[i];  // (p1, p2, m1, m2)
+        P[i] = fmaf(h00, k.x, fmaf(h01, k.y, fmaf(h10, k.z, h11 * k.w)));
     }
     for (unsigned i = threadIdx.x; i < 256; i += blockDim.x) {
         float hsv[3];
         for (int j = 0; j < 3; j++) {
-            float4 k = seg[RFK_SIZE_REALS + 3 * i + j];
-            hsv[j] = fmaf(fmaf(fmaf(k.x, t, k.y), t, k.z), t, k.w);
+            const float4 k = seg[RFK_SIZE_REALS + 3 * i + j];
+            hsv[j] = fmaf(h00, k.x, fmaf(h01, k.y, fmaf(h10, k.z, h11 * k.w)));
         }
         // HSV -> RGB as refactor.cu:128-140, truncated to 8 bits
         float rgb[3];
@@ -341,7 +343,8 @@ struct rfk_bin_args {
     float4* bins;
     unsigned w, h;
     unsigned seed, salt;
-    unsigned call_id, pad0;             // call_id selects this call's Philox sub-stream
+    unsigned call_id;                   // selects this call's Philox sub-stream
+    unsigned check;                     // passes between bailout checks
     unsigned long long quality_target;  // stop when counters->quality >= this (0 = no target)
     unsigned long long max_passes;      // per-chain cap for this call (0 = no cap)
     unsigned long long time_ns;         // time budget per block (0 = none)
@@ -385,7 +388,7 @@ extern "C" __global__ void __launch_bounds__(RFK_BLOCK) rfk_bin(rfk_bin_args a) 
 #pragma unroll 1
     for (;;) {
 #pragma unroll 1
-        for (int it = 0; it < RFK_CHECK; it++) {
+        for (unsigned it = 0; it < a.check && (a.max_passes == 0 || pass < a.max_passes); it++) {
 #pragma unroll
             for (int k = 0; k < RFK_CPT; k++) {
                 Rng rng;

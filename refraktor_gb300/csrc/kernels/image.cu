@@ -13,7 +13,8 @@ namespace {
 // ------------------------------------------------------------ Catmull-Rom --
 // Centripetal Catmull-Rom (alpha = 0.5, tension 0) segment p1 -> p2 with knot
 // distance sqrt(hypot(dp, 1)), as assets/kernels/catmull.cu:11-28, evaluated
-// in FP32 from the FP64 packed samples. One thread per (segment, real).
+// in FP32 from the FP64 packed samples and stored in Hermite form
+// (p1, p2, m1, m2). One thread per (segment, real).
 __global__ void __launch_bounds__(256) catmull_kernel(const double* __restrict__ samples, unsigned sample_size,
                                                       unsigned nseg, float4* __restrict__ coeff) {
     const unsigned long long i = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x;
@@ -27,12 +28,9 @@ __global__ void __launch_bounds__(256) catmull_kernel(const double* __restrict__
     const float t23 = sqrtf(hypotf(p3 - p2, 1.0f));
     const float m1 = p2 - p1 + t12 * ((p1 - p0) / t01 - (p2 - p0) / (t01 + t12));
     const float m2 = p2 - p1 + t12 * ((p3 - p2) / t23 - (p3 - p1) / (t12 + t23));
-    float4 k;
-    k.x = 2.0f * (p1 - p2) + m1 + m2;
-    k.y = -3.0f * (p1 - p2) - m1 - m1 - m2;
-    k.z = m1;
-    k.w = p1;
-    coeff[i] = k;
+    // Hermite form: a = 2(p1-p2)+m1+m2, b = -3(p1-p2)-2m1-m2, c = m1, d = p1
+    // of the reference describe the same cubic
+    coeff[i] = make_float4(p1, p2, m1, m2);
 }
 
 // ----------------------------------------------------------------- tonemap --

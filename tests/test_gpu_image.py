@@ -142,7 +142,17 @@ def test_density_blur_matches_oracle(max_r, min_r, curve):
     assert got[..., 3].sum() <= bins[..., 3].sum() * (1 + 1e-5)
 
 
-def test_catmull_coefficients_match_oracle():
+T_VALUES = [0.0, 0.1, 0.25, 0.5, 0.77, 0.999, 1.0]
+
+
+def _curve_scale(samples, n, nseg):
+    p = samples.reshape(nseg + 3, n)
+    return np.stack([np.abs(p[s:s + 4]).max(axis=0) for s in range(nseg)])
+
+
+def test_catmull_segments_match_oracle():
+    """FP32 Hermite segments evaluated at t vs the FP64 cubic of catmull.cu:
+    within 4 FP32 ulps of the segment's largest control point."""
     rng = np.random.default_rng(6)
     n, nseg = 1000, 2
     samples = rng.uniform(-5, 5, size=(nseg + 3) * n)
@@ -152,11 +162,13 @@ def test_catmull_coefficients_match_oracle():
     lr.catmull_coefficients(d_s, n, nseg, d_c)
     got = d_c.cpu().numpy().astype(np.float64)
     ref = orc.catmull(samples, n)
-    # coefficients combine differences of the control points: tolerance 8 FP32
-    # ulps of the largest control point magnitude of each real
+    tol = 4 * np.spacing(_curve_scale(samples, n, nseg).astype(np.float32)).astype(np.float64)
+    for t in T_VALUES:
+        assert np.all(np.abs(orc.hermite_eval(got, t) - orc.cubic_eval(ref, t)) <= tol), t
+    # knots are reproduced exactly (up to the FP32 rounding of the sample)
     p = samples.reshape(nseg + 3, n)
-    scale = np.stack([np.abs(p[s:s + 4]).max(axis=0) for s in range(nseg)])[..., None]
-    assert np.all(np.abs(got - ref) <= 8 * np.spacing(scale.astype(np.float32)).astype(np.float64))
+    np.testing.assert_array_equal(got[..., 0], p[1:nseg + 1].astype(np.float32))
+    np.testing.assert_array_equal(got[..., 1], p[2:nseg + 2].astype(np.float32))
 
 
 @pytest.mark.skipif(not refkernels.available("catmull"), reason="reference kernels not built")
@@ -174,8 +186,9 @@ def test_catmull_matches_reference_kernel():
     a = mine.cpu().numpy().astype(np.float64)
     b = theirs.cpu().numpy()
     np.testing.assert_allclose(b, orc.catmull(samples, n), rtol=1e-12, atol=1e-12)  # reference kernel == oracle (FP64)
-    scale = np.abs(samples.reshape(nseg + 3, n)).max(axis=0)[None, :, None]
-    assert np.all(np.abs(a - b) <= 8 * np.spacing(scale.astype(np.float32)).astype(np.float64))
+    tol = 4 * np.spacing(_curve_scale(samples, n, nseg).astype(np.float32)).astype(np.float64)
+    for t in T_VALUES:
+        assert np.all(np.abs(orc.hermite_eval(a, t) - orc.cubic_eval(b, t)) <= tol), t
 
 
 def test_red_v4_probe_runs():
