@@ -84,9 +84,10 @@ uint64_t rfk_flame_structure_hash(const rfk_flame* f);
 typedef struct {
     int precise_math;      /* 0: -use_fast_math as the reference (flame_compiler.cpp:861); 1: full-precision libm */
     int block;             /* threads per block (0 = 256) */
-    int chains_per_thread; /* 0 = 1 */
+    int chains_per_thread; /* 0 = 4 when sorting, else 1 */
     int flush;             /* histogram update: 0 = red.global.add.v4.f32 per draw, 1 = warp-aggregated */
     int blocks_per_sm;     /* 0 = as many as fit */
+    int sort;              /* 0 = sort each warp's chains by xform when 2..32 xforms; -1 = never */
 } rfk_compile_opts;
 
 typedef struct {
@@ -94,6 +95,7 @@ typedef struct {
     int block;
     int chains_per_thread;
     int flush;
+    int sort;               /* 1 when chains are sorted by xform every pass */
     int registers;          /* of the bin kernel */
     int num_xforms;
     int has_final;

@@ -256,6 +256,22 @@ double oracle_apply(const int* structure, const double* params, int xf, double* 
     return apply_xf(&d, params, xf, x, y, c, u, used);
 }
 
+void oracle_apply_many(const int* structure, const double* params, int xf, size_t n, const double* in_xyc,
+                       double* out_xyco) {
+    flame_desc d;
+    if (parse_structure(structure, &d) < 0) return;
+    const double u[40] = {0};
+    for (size_t i = 0; i < n; i++) {
+        double x = in_xyc[3 * i], y = in_xyc[3 * i + 1], c = in_xyc[3 * i + 2];
+        int used = 0;
+        const double op = apply_xf(&d, params, xf, &x, &y, &c, u, &used);
+        out_xyco[4 * i] = x;
+        out_xyco[4 * i + 1] = y;
+        out_xyco[4 * i + 2] = c;
+        out_xyco[4 * i + 3] = op;
+    }
+}
+
 /* -------------------------------------------------------------- RNG (xoshiro256**) */
 typedef struct { uint64_t s[4]; } rng_t;
 
@@ -299,6 +315,8 @@ typedef struct {
     uint64_t seed;
     const double* jitter; /* n_jitter x 2 */
     int n_jitter;
+    uint64_t n_chains;
+    int hammersley;
     double* hist;
     uint64_t draws;
     double wsum;
@@ -327,8 +345,32 @@ static void* render_job(void* arg) {
     for (uint64_t ch = j->chain_begin; ch < j->chain_end; ch++) {
         rng_t r;
         rng_seed(&r, j->seed * 0x100000001B3ull + ch);
-        /* start: uniform over the image, mapped through the plane-space affine */
-        const double sx0 = u01(&r) * j->w, sy0 = u01(&r) * j->h;
+        /* start: over the image, mapped through the plane-space affine; either
+           uniform or the Hammersley point of refactor.cu:39-54, :301-304 */
+        double sx0, sy0;
+        if (j->hammersley) {
+            const uint32_t total = (uint32_t)j->n_chains, idx = (uint32_t)ch;
+            uint32_t max_val = total;
+            if (total % 2u) {
+                max_val = 1;
+                while (max_val < total) max_val <<= 1;
+            }
+            uint32_t radix = 0, v = max_val;
+            while (v >>= 1) radix++;
+            uint32_t rev = idx;
+            rev = (rev << 16) | (rev >> 16);
+            rev = ((rev & 0x00ff00ffu) << 8) | ((rev & 0xff00ff00u) >> 8);
+            rev = ((rev & 0x0f0f0f0fu) << 4) | ((rev & 0xf0f0f0f0u) >> 4);
+            rev = ((rev & 0x33333333u) << 2) | ((rev & 0xccccccccu) >> 2);
+            rev = ((rev & 0x55555555u) << 1) | ((rev & 0xaaaaaaaau) >> 1);
+            const uint32_t flipped = radix ? rev >> (32 - radix) : 0;
+            const double inv = 1.0 / max_val;
+            sx0 = ((idx * inv * 2.0 - 1.0) + 1.0) / 2.0 * j->w;
+            sy0 = ((flipped * inv * 2.0 - 1.0) + 1.0) / 2.0 * j->h;
+        } else {
+            sx0 = u01(&r) * j->w;
+            sy0 = u01(&r) * j->h;
+        }
         double x = P[6] * sx0 + P[8] * sy0 + P[10];
         double y = P[7] * sx0 + P[9] * sy0 + P[11];
         double c = u01(&r);
@@ -371,7 +413,7 @@ static void* render_job(void* arg) {
 
 uint64_t oracle_render(const int* structure, const double* params, const double* pal, uint32_t w, uint32_t h,
                        uint64_t n_chains, uint32_t warmup, uint64_t passes, uint64_t seed, int threads, int n_jitter,
-                       const double* jitter_in, double* hist) {
+                       const double* jitter_in, int hammersley, double* hist) {
     flame_desc* d = (flame_desc*)malloc(sizeof(flame_desc));
     if (!d || parse_structure(structure, d) < 0 || d->chaos) {
         free(d);
@@ -413,6 +455,8 @@ uint64_t oracle_render(const int* structure, const double* params, const double*
         j->seed = seed;
         j->jitter = jit;
         j->n_jitter = n_jitter;
+        j->n_chains = n_chains;
+        j->hammersley = hammersley;
         j->hist = (t == 0) ? hist : (double*)calloc(hsz, sizeof(double));
         j->wsum = wsum;
         double run = 0.0;

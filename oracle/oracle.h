@@ -70,11 +70,17 @@ double oracle_apply(const int* structure, const double* params, int xf, double* 
  * `passes` drawing passes, into hist [h][w][4] (doubles, summed). The screen
  * affine of chain i gets offset i % n_jitter of `jitter` (n_jitter x 2), or
  * when `jitter` is NULL, of n_jitter Gaussian(1/3 px) offsets it draws
- * (flame.tpl:179-182). Runs on `threads` POSIX threads. Returns the number
- * of draws. */
+ * (flame.tpl:179-182). Chains start uniformly over the image, or with
+ * `hammersley` at Hammersley point i of n_chains (refactor.cu:39-54,
+ * :301-304). Runs on `threads` POSIX threads. Returns the number of draws. */
 uint64_t oracle_render(const int* structure, const double* params, const double* palette_rgb, uint32_t w, uint32_t h,
                        uint64_t n_chains, uint32_t warmup, uint64_t passes, uint64_t seed, int threads, int n_jitter,
-                       const double* jitter, double* hist);
+                       const double* jitter, int hammersley, double* hist);
+
+/* oracle_apply over n points (x, y, c) -> (x, y, c, opacity), with every
+ * random draw 0. */
+void oracle_apply_many(const int* structure, const double* params, int xf, size_t n, const double* in_xyc,
+                       double* out_xyco);
 
 /* tonemap (tonemap.cu:67-104, tonemapper.cpp:52) in FP64: bins [n][4] ->
  * out [n][4] (alpha in the 4th channel). highlight_power < 0 = off. */

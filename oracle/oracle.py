@@ -48,7 +48,8 @@ def lib() -> C.CDLL:
                                    C.POINTER(C.c_double), C.c_void_p, C.POINTER(C.c_int)]
         L.oracle_apply.restype = C.c_double
         L.oracle_render.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_uint32, C.c_uint32, C.c_uint64, C.c_uint32,
-                                    C.c_uint64, C.c_uint64, C.c_int, C.c_int, C.c_void_p, C.c_void_p]
+                                    C.c_uint64, C.c_uint64, C.c_int, C.c_int, C.c_void_p, C.c_int, C.c_void_p]
+        L.oracle_apply_many.argtypes = [C.c_void_p, C.c_void_p, C.c_int, C.c_size_t, C.c_void_p, C.c_void_p]
         L.oracle_render.restype = C.c_uint64
         L.oracle_tonemap.argtypes = [C.c_void_p, C.c_size_t, C.c_double, C.c_double, C.c_double, C.c_double, C.c_double,
                                      C.c_void_p]
@@ -219,7 +220,8 @@ def apply(g: dict, params: np.ndarray, xf: int, x: float, y: float, c: float, u=
 
 
 def render(g: dict, w: int, h: int, chains: int, passes: int, warmup: int = 20, seed: int = 1, threads: int = 1,
-           n_jitter: int = 1024, params=None, palette=None, jitter=None) -> tuple[np.ndarray, int]:
+           n_jitter: int = 1024, params=None, palette=None, jitter=None, hammersley: bool = False
+           ) -> tuple[np.ndarray, int]:
     """FP64 chaos game. `jitter` (n x 2) gives the screen offsets to cycle
     over the chains; by default n_jitter Gaussian(1/3 px) offsets are drawn."""
     if params is None:
@@ -234,8 +236,18 @@ def render(g: dict, w: int, h: int, chains: int, passes: int, warmup: int = 20, 
         n_jitter = j.shape[0]
         jp = j.ctypes.data
     draws = lib().oracle_render(s.ctypes.data, P.ctypes.data, pal.ctypes.data, w, h, chains, warmup, passes, seed, threads,
-                                n_jitter, jp, hist.ctypes.data)
+                                n_jitter, jp, 1 if hammersley else 0, hist.ctypes.data)
     return hist, int(draws)
+
+
+def apply_many(g: dict, params: np.ndarray, xf: int, pts: np.ndarray) -> np.ndarray:
+    """oracle_apply over an (n, 3) array of (x, y, colour); random draws are 0."""
+    s = structure(g)
+    P = np.ascontiguousarray(params, dtype=np.float64)
+    p = np.ascontiguousarray(pts, dtype=np.float64)
+    out = np.zeros((p.shape[0], 4))
+    lib().oracle_apply_many(s.ctypes.data, P.ctypes.data, xf, p.shape[0], p.ctypes.data, out.ctypes.data)
+    return out
 
 
 def hermite_eval(seg4: np.ndarray, t: float) -> np.ndarray:

@@ -15,12 +15,12 @@ c_size_p = C.POINTER(C.c_size_t)
 
 class CompileOpts(C.Structure):
     _fields_ = [("precise_math", C.c_int), ("block", C.c_int), ("chains_per_thread", C.c_int), ("flush", C.c_int),
-                ("blocks_per_sm", C.c_int)]
+                ("blocks_per_sm", C.c_int), ("sort", C.c_int)]
 
 
 class KernelInfo(C.Structure):
     _fields_ = [("grid", C.c_int), ("block", C.c_int), ("chains_per_thread", C.c_int), ("flush", C.c_int),
-                ("registers", C.c_int), ("num_xforms", C.c_int), ("has_final", C.c_int), ("chaos", C.c_int),
+                ("sort", C.c_int), ("registers", C.c_int), ("num_xforms", C.c_int), ("has_final", C.c_int), ("chaos", C.c_int),
                 ("size_reals", C.c_size_t), ("sample_floats", C.c_size_t), ("compile_ms", C.c_double),
                 ("sfu_per_iter", C.c_double)]
 

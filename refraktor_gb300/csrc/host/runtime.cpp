@@ -127,7 +127,7 @@ struct kernel_impl {
     std::string log;
     cudaLibrary_t lib = nullptr;
     cudaKernel_t f_prepare = nullptr, f_warmup = nullptr, f_bin = nullptr, f_apply = nullptr;
-    int block = 256, cpt = 1, flush = 0, grid = 0, regs = 0;
+    int block = 256, cpt = 1, flush = 0, sort = 0, grid = 0, regs = 0;
     size_t sample_floats = 0;
     double compile_ms = 0.0;
     double sfu_per_iter = 0.0;
@@ -186,13 +186,14 @@ std::string full_source(const rfk::generated_flame& g) {
 }
 
 std::vector<char> nvrtc_build(const std::string& source, const std::string& arch_name, const rfk_compile_opts& o, int block,
-                              int cpt, int flush, std::string& log) {
+                              int cpt, int flush, int sort, std::string& log) {
     const std::string arch = "--gpu-architecture=" + arch_name;
     const std::string d_block = "-DRFK_BLOCK=" + std::to_string(block);
     const std::string d_cpt = "-DRFK_CPT=" + std::to_string(cpt);
     const std::string d_flush = "-DRFK_FLUSH=" + std::to_string(flush);
+    const std::string d_sort = "-DRFK_SORT=" + std::to_string(sort);
     std::vector<const char*> opts = {arch.c_str(), "-std=c++17", "-lineinfo", d_block.c_str(), d_cpt.c_str(),
-                                     d_flush.c_str(), "-extra-device-vectorization"};
+                                     d_flush.c_str(), d_sort.c_str(), "-extra-device-vectorization"};
     if (!o.precise_math) opts.push_back("--use_fast_math");
     nvrtcProgram prog;
     if (nvrtcCreateProgram(&prog, source.c_str(), "rfk_flame.cu", 0, nullptr, nullptr) != NVRTC_SUCCESS)
@@ -216,6 +217,19 @@ std::vector<char> nvrtc_build(const std::string& source, const std::string& arch
     return cubin;
 }
 
+// Sorting chains by xform pays off when there is more than one xform and the
+// per-xform ballots stay few (sort = 0 in the options means this choice).
+int resolve_sort(const rfk_compile_opts& o, size_t nx) {
+    const bool can = nx >= 2 && nx <= 32;
+    if (o.sort < 0) return 0;
+    return can ? 1 : 0;
+}
+
+int resolve_cpt(const rfk_compile_opts& o, int sort) {
+    if (o.chains_per_thread > 0) return o.chains_per_thread;
+    return sort ? 4 : 1;
+}
+
 void check_options(const rfk_compile_opts& o) {
     const int block = o.block > 0 ? o.block : 256;
     if (block % 32 != 0 || block > 1024) fail(RFK_E_INVALID, "block must be a multiple of 32 up to 1024");
@@ -232,8 +246,10 @@ std::shared_ptr<kernel_impl> compile(const rfk::flamedb& db, const rfk::flame& f
     const auto t0 = std::chrono::steady_clock::now();
     auto k = std::make_shared<kernel_impl>();
     k->gen = rfk::generate_flame_code(db, f);
+    check_options(o);
     k->block = o.block > 0 ? o.block : 256;
-    k->cpt = o.chains_per_thread > 0 ? o.chains_per_thread : 1;
+    k->sort = resolve_sort(o, k->gen.num_xforms);
+    k->cpt = resolve_cpt(o, k->sort);
     k->flush = o.flush;
     check_options(o);
     k->sample_floats = sample_floats_for(k->gen);
@@ -242,7 +258,7 @@ std::shared_ptr<kernel_impl> compile(const rfk::flamedb& db, const rfk::flame& f
 
     k->source = full_source(k->gen);
 
-    std::vector<char> cubin = nvrtc_build(k->source, device_arch(), o, k->block, k->cpt, k->flush, log);
+    std::vector<char> cubin = nvrtc_build(k->source, device_arch(), o, k->block, k->cpt, k->flush, k->sort, log);
     cuda_check(cudaLibraryLoadData(&k->lib, cubin.data(), nullptr, nullptr, 0, nullptr, nullptr, 0), "cudaLibraryLoadData");
     cuda_check(cudaLibraryGetKernel(&k->f_prepare, k->lib, "rfk_prepare"), "rfk_prepare");
     cuda_check(cudaLibraryGetKernel(&k->f_warmup, k->lib, "rfk_warmup"), "rfk_warmup");
@@ -274,7 +290,7 @@ std::shared_ptr<kernel_impl> compile_cached(const rfk::flamedb& db, const rfk::f
                                            std::string& log) {
     std::ostringstream key;
     key << db.hash() << "|" << f.structure_key() << "|" << o.precise_math << "," << o.block << "," << o.chains_per_thread
-        << "," << o.flush << "," << o.blocks_per_sm;
+        << "," << o.flush << "," << o.blocks_per_sm << "," << o.sort;
     {
         std::lock_guard<std::mutex> lk(g_cache_mu);
         auto it = g_cache.find(key.str());
@@ -515,8 +531,8 @@ rfk_status rfk_compile_check(const rfk_db* db, const rfk_flame* f, const rfk_com
         if (opts) o = *opts;
         check_options(o);
         auto g = rfk::generate_flame_code(db->db, f->f);
-        nvrtc_build(full_source(g), arch, o, o.block > 0 ? o.block : 256, o.chains_per_thread > 0 ? o.chains_per_thread : 1,
-                    o.flush, nlog);
+        const int sort = resolve_sort(o, g.num_xforms);
+        nvrtc_build(full_source(g), arch, o, o.block > 0 ? o.block : 256, resolve_cpt(o, sort), o.flush, sort, nlog);
     });
     if (log && log_cap) copy_out(log, log_cap, nullptr, st == RFK_OK ? nlog : g_error);
     return st;
@@ -530,6 +546,7 @@ rfk_status rfk_kernel_get_info(const rfk_kernel* kh, rfk_kernel_info* out) {
         out->block = k.block;
         out->chains_per_thread = k.cpt;
         out->flush = k.flush;
+        out->sort = k.sort;
         out->registers = k.regs;
         out->num_xforms = (int)k.gen.num_xforms;
         out->has_final = k.gen.has_final;

@@ -183,6 +183,14 @@ struct Rng {
         k0 = key0; k1 = key1;
         refill();
     }
+    // As start(), but the first block is generated on the first draw: a chain
+    // step whose variations draw nothing costs no Philox rounds.
+    RFK_FN void start_lazy(rfk_u32 stream, rfk_u32 sub, rfk_u64 pass, rfk_u32 key0, rfk_u32 key1) {
+        ctr.x = stream; ctr.y = sub; ctr.z = (rfk_u32)pass; ctr.w = (rfk_u32)(pass >> 32);
+        k0 = key0; k1 = key1;
+        b0 = b1 = b2 = b3 = 0u;
+        left = 0;
+    }
     RFK_FN void refill() {
         rfk_u32x4 r = rfk_philox(ctr, k0, k1);
         b0 = r.x; b1 = r.y; b2 = r.z; b3 = r.w; left = 4;

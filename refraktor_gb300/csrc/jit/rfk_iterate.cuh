@@ -9,7 +9,9 @@
 //   void rfk_precalc(float* P, Rng& rng)                             (variation precalc)
 // and the launch shape: RFK_BLOCK (threads per block), RFK_CPT (chains per
 // thread), RFK_FLUSH (0 = one red.global.add.v4.f32 per draw, 1 = warp-
-// aggregated red for lanes that hit the same pixel).
+// aggregated red for lanes that hit the same pixel), RFK_SORT (1 = sort each
+// warp's chains by picked xform every pass, so a warp runs one xform at a
+// time instead of a divergent switch).
 //
 // Reference behaviour restated here (assets/kernels/refactor.cu):
 //   :99-117,:266-294  per temporal sample: flame = Catmull-Rom at t, affines
@@ -35,6 +37,9 @@
 #endif
 #ifndef RFK_FLUSH
 #define RFK_FLUSH 0
+#endif
+#ifndef RFK_SORT
+#define RFK_SORT 0
 #endif
 
 // Per-sample parameter block (floats).
@@ -205,15 +210,11 @@ __device__ __forceinline__ int rfk_pick(float u, const float* __restrict__ P, un
     return k;
 }
 
-// One chaos-game step of one chain. Returns the draw (pixel index or -1) and
-// its RGBA contribution.
-__device__ __forceinline__ int rfk_step(float& x, float& y, float& c, unsigned& last, Rng& rng,
-                                        const float* __restrict__ P, unsigned w, unsigned h, float4& contrib,
-                                        unsigned& hit) {
-    const int k = rfk_pick(rng.u01(), P, last);
-#if RFK_CHAOS
-    last = (unsigned)k;
-#endif
+// Moves one chain through xform k: apply, bad-value reset, final xform on a
+// copy, screen projection. Returns the draw (pixel index or -1) and its RGBA
+// contribution.
+__device__ __forceinline__ int rfk_move(int k, float& x, float& y, float& c, Rng& rng, const float* __restrict__ P,
+                                        unsigned w, unsigned h, float4& contrib, unsigned& hit) {
     V2 p = fl_vec2(x, y);
     R col = c;
     R op = rfk_dispatch(k, p, col, P, rng);
@@ -250,6 +251,55 @@ __device__ __forceinline__ int rfk_step(float& x, float& y, float& c, unsigned& 
     }
     return -1;
 }
+
+// One chaos-game step of one chain: pick an xform from the cumulative weights
+// (or the chaos row of the previous xform), then move.
+__device__ __forceinline__ int rfk_step(float& x, float& y, float& c, unsigned& last, Rng& rng,
+                                        const float* __restrict__ P, unsigned w, unsigned h, float4& contrib,
+                                        unsigned& hit) {
+    const int k = rfk_pick(rng.u01(), P, last);
+#if RFK_CHAOS
+    last = (unsigned)k;
+#endif
+    return rfk_move(k, x, y, c, rng, P, w, h, contrib, hit);
+}
+
+#if RFK_SORT
+// Counting sort of a warp's 32 * RFK_CPT chains by their picked xform,
+// through the warp's stage buffer in shared memory: afterwards round q of
+// every lane holds sorted slot q * 32 + lane, so the lanes of one round run
+// the same xform except at the boundaries between xform runs. Ranks come from
+// one ballot per (xform, round); only __syncwarp is needed.
+__device__ __forceinline__ void rfk_sort_chains(float (&x)[RFK_CPT], float (&y)[RFK_CPT], float (&c)[RFK_CPT],
+                                                int (&k)[RFK_CPT], float4* __restrict__ stage) {
+    const unsigned lane = threadIdx.x & 31u;
+    const unsigned lt = (1u << lane) - 1u;
+    unsigned pos[RFK_CPT];
+    unsigned base = 0;
+#pragma unroll
+    for (int j = 0; j < RFK_NX; j++) {
+#pragma unroll
+        for (int q = 0; q < RFK_CPT; q++) {
+            const bool mine = (k[q] == j);
+            const unsigned b = __ballot_sync(0xffffffffu, mine);
+            if (mine) pos[q] = base + __popc(b & lt);
+            base += __popc(b);
+        }
+    }
+#pragma unroll
+    for (int q = 0; q < RFK_CPT; q++) stage[pos[q]] = make_float4(x[q], y[q], c[q], __int_as_float(k[q]));
+    __syncwarp();
+#pragma unroll
+    for (int q = 0; q < RFK_CPT; q++) {
+        const float4 v = stage[q * 32 + lane];
+        x[q] = v.x;
+        y[q] = v.y;
+        c[q] = v.z;
+        k[q] = __float_as_int(v.w);
+    }
+    __syncwarp();
+}
+#endif
 
 __device__ __forceinline__ void rfk_flush(float4* __restrict__ bins, int idx, float4 v) {
 #if RFK_FLUSH == 1
@@ -357,6 +407,11 @@ extern "C" __global__ void __launch_bounds__(RFK_BLOCK) rfk_bin(rfk_bin_args a) 
     __shared__ unsigned long long s_hits, s_draws;
     __shared__ unsigned s_bail;
     __shared__ unsigned long long s_start;
+#if RFK_SORT
+    __shared__ float4 s_stage[RFK_BLOCK / 32][32 * RFK_CPT];
+    float4* stage = s_stage[threadIdx.x >> 5];
+    const unsigned lane_stream = blockIdx.x * RFK_BLOCK + threadIdx.x;
+#endif
     const float* src = a.samples + (size_t)blockIdx.x * RFK_SAMPLE_FLOATS;
     for (unsigned i = threadIdx.x; i < RFK_SAMPLE_FLOATS; i += RFK_BLOCK) P[i] = src[i];
     if (threadIdx.x == 0) {
@@ -389,6 +444,29 @@ extern "C" __global__ void __launch_bounds__(RFK_BLOCK) rfk_bin(rfk_bin_args a) 
     for (;;) {
 #pragma unroll 1
         for (unsigned it = 0; it < a.check && (a.max_passes == 0 || pass < a.max_passes); it++) {
+#if RFK_SORT
+            // picks of this lane's chains from one Philox stream per lane
+            Rng pr;
+            pr.start_lazy(lane_stream, a.call_id, pass, a.seed, a.salt ^ 0x9E3779B9u);
+            int kk[RFK_CPT];
+#pragma unroll
+            for (int k = 0; k < RFK_CPT; k++) kk[k] = rfk_pick(pr.u01(), P, last[k]);
+            rfk_sort_chains(x, y, c, kk, stage);
+#pragma unroll
+            for (int k = 0; k < RFK_CPT; k++) {
+#if RFK_CHAOS
+                last[k] = (unsigned)kk[k];
+#endif
+                Rng rng;
+                rng.start_lazy(chain[k], a.call_id, pass, a.seed, a.salt);
+                float4 v;
+                unsigned hit;
+                int idx = rfk_move(kk[k], x[k], y[k], c[k], rng, P, a.w, a.h, v, hit);
+                rfk_flush(a.bins, idx, v);
+                my_hits += hit;
+                my_draws += (idx >= 0) ? 1u : 0u;
+            }
+#else
 #pragma unroll
             for (int k = 0; k < RFK_CPT; k++) {
                 Rng rng;
@@ -400,6 +478,7 @@ extern "C" __global__ void __launch_bounds__(RFK_BLOCK) rfk_bin(rfk_bin_args a) 
                 my_hits += hit;
                 my_draws += (idx >= 0) ? 1u : 0u;
             }
+#endif
             pass++;
         }
         // bailout check: block totals -> global counters -> decision

@@ -69,26 +69,50 @@ def _xform(rng: np.random.Generator, weight: float, names: list[str]) -> dict:
     }
 
 
+def _quantile_box(dens: np.ndarray, g: dict, rw: int, rh: int, q: float = 0.01):
+    """Plane-space box holding the q..1-q mass of a low-resolution render."""
+    col = dens.sum(axis=0)
+    row = dens.sum(axis=1)
+    if col.sum() <= 0:
+        return None
+
+    def qi(m):
+        c = np.cumsum(m) / m.sum()
+        return int(np.searchsorted(c, q)), int(np.searchsorted(c, 1 - q))
+
+    x0, x1 = qi(col)
+    y0, y1 = qi(row)
+    s = g["scale"] * rh
+    to_x = lambda px: (px - rw / 2.0) / s + g["center_x"]  # noqa: E731
+    to_y = lambda py: (py - rh / 2.0) / s + g["center_y"]  # noqa: E731
+    return to_x(x0), to_x(x1 + 1), to_y(y0), to_y(y1 + 1)
+
+
 def frame_on_gpu(db, genome: dict, w: int, h: int, seed: int = 0) -> dict:
-    """Refits centre and scale so that the 1%..99% box of the attractor fills
-    the image, from the chain positions after a warm-up on the GPU."""
+    """Refits centre and scale so that the 1%..99% box of the drawn points
+    (after the final xform) fills the image: a wide low-resolution render on
+    the GPU locates the attractor, a second one at the located box refines it."""
     from . import librefrakt as lr
 
-    f = lr.flame.from_json(db, genome)
-    k = lr.flame_compiler().get_flame_kernel(db, f)
-    st = k.warmup(f.pack_samples(4, w, h), (w, h), seed, 64)
-    xy = st.chains()[:2].T
-    xy = xy[np.all(np.isfinite(xy), axis=1)]
-    out = dict(genome)
-    if xy.shape[0] < 16:
-        return out
-    lo = np.quantile(xy, 0.01, axis=0)
-    hi = np.quantile(xy, 0.99, axis=0)
-    cx, cy = (lo + hi) / 2.0
-    span_x, span_y = max(hi[0] - lo[0], 1e-3), max(hi[1] - lo[1], 1e-3)
-    # screen = (p - centre) * scale * h + (w/2, h/2): fit both extents, 5% margin
-    out["center_x"], out["center_y"] = float(cx), float(cy)
-    out["scale"] = float(min(w / (span_x * h), 1.0 / span_y) * 0.95)
+    rw = 256
+    rh = max(16, int(round(rw * h / w)))
+    g = dict(genome, center_x=0.0, center_y=0.0, scale=1.0 / 40.0)  # view spans 40 units vertically
+    comp = lr.flame_compiler()
+    for _ in range(2):
+        f = lr.flame.from_json(db, g)
+        k = comp.get_flame_kernel(db, f)
+        st = k.warmup(f.pack_samples(4, rw, rh), (rw, rh), seed, 64)
+        k.bin(st, lr.bailout_args(iters=0, millis=2000, quality=16.0))
+        box = _quantile_box(st.bins()[..., 3].double().cpu().numpy(), g, rw, rh)
+        if box is None:
+            return dict(genome)
+        x0, x1, y0, y1 = box
+        span_x, span_y = max(x1 - x0, 1e-4), max(y1 - y0, 1e-4)
+        # screen = (p - centre) * scale * h + (w/2, h/2): fit both extents, 5% margin
+        g = dict(g, center_x=float((x0 + x1) / 2), center_y=float((y0 + y1) / 2),
+                 scale=float(min(rw / (span_x * rh), 1.0 / span_y) * 0.95))
+    out = dict(genome, center_x=g["center_x"], center_y=g["center_y"],
+               scale=float(g["scale"]) * (rh / rw) / (h / w))
     return out
 
 

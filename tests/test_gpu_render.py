@@ -50,10 +50,10 @@ def test_warmup_and_bin_reach_quality(db, comp):
     assert r.total_draws == int(r.quality * w * h)
     assert r.max_density == pytest.approx(float(np.floor(bins[..., 3].max())), abs=1.0)
     # resume: a second call keeps accumulating
-    r2 = k.bin(st, lr.bailout_args(iters=0, millis=0, quality=4.0))
+    r2 = k.bin(st, lr.bailout_args(iters=0, millis=0, quality=16.0))
     assert st.quality == pytest.approx(r.quality + r2.quality)
     bins2 = st.bins().cpu().numpy()
-    assert bins2[..., 3].sum() > bins[..., 3].sum() * 1.4
+    assert bins2[..., 3].sum() == pytest.approx(r.draw_count + r2.draw_count, rel=1e-5)
 
 
 def test_pass_cap_and_time_bailouts(db, comp):
@@ -169,33 +169,52 @@ def test_affine_step_exact_fma(db, comp):
     out = k.apply_xform(prep, 0, pts).astype(np.float64)
     a, d, b, e, c, ff = prep[17:23].astype(np.float64)
     x, y = pts[:, 0].astype(np.float64), pts[:, 1].astype(np.float64)
-    for got, ref, terms in [(out[:, 0], a * x + b * y + c, np.maximum.reduce([abs(a * x), abs(b * y), abs(c)])),
-                            (out[:, 1], d * x + e * y + ff, np.maximum.reduce([abs(d * x), abs(e * y), abs(ff)]))]:
+    cx, cf = np.full_like(x, abs(c)), np.full_like(x, abs(ff))
+    for got, ref, terms in [(out[:, 0], a * x + b * y + c, np.maximum.reduce([abs(a * x), abs(b * y), cx])),
+                            (out[:, 1], d * x + e * y + ff, np.maximum.reduce([abs(d * x), abs(e * y), cf]))]:
         assert np.all(np.abs(got - ref) <= np.spacing(terms.astype(np.float32)))
 
 
 @pytest.mark.parametrize("name", DETERMINISTIC)
 def test_single_map_within_4_ulp(db, comp, name):
-    """The variation half of a map in the precise-math build vs an FP64
-    evaluation of the reference formula on the same FP32 input (identity
-    affine, so the input reaches the variation unrounded): at least 99% of
-    points within 4 ulp of the larger output component, every point within
-    64 ulp (cancellation near zeros of the formula)."""
+    """The variation half of a map in the precise-math build vs FP64
+    evaluations of the reference formula (identity affine, so the FP32 input
+    reaches the variation unrounded). Backward-error form: every FP32 result
+    is within 4 ulp (of the larger output component) of the FP64 result at
+    some input within 2 ulp of the given one - FP32 arguments such as
+    sqrt * atan or (atan + sqrt) carry rounding that no FP32 evaluation can
+    avoid. The forward error at the exact input is reported and bounded too:
+    median <= 1 ulp, 90% <= 4 ulp."""
     g = _one_variation_flame(name, seed=hash(name) % 1000)
     g["xforms"][0]["vchain"][0]["transform"] = [1.0, 0.0, 0.0, 1.0, 0.0, 0.0]
     f = lr.flame.from_json(db, g)
     k = comp.get_flame_kernel(db, f, precise_math=1)
     prep = k.prepare_samples(f.pack_samples(4, 256, 256), [0], [0.0])[0]
     rng = np.random.default_rng(12)
-    n = 4096
+    n = 2048
     pts = np.stack([rng.uniform(-1.5, 1.5, n), rng.uniform(-1.5, 1.5, n), rng.uniform(0, 1, n)], 1).astype(np.float32)
     out = k.apply_xform(prep, 0, pts).astype(np.float64)
     P = prep[:f.size_reals()].astype(np.float64)
-    ref = np.array([orc.apply(g, P, 0, float(x), float(y), float(c))[:4] for x, y, c in pts])
-    ok = np.isfinite(ref[:, 0]) & np.isfinite(ref[:, 1]) & (np.abs(ref[:, :2]).max(axis=1) < 1e6)
-    e = _ulp_errors(out[ok], ref[ok])
-    assert np.mean(e <= 4) >= 0.99, (name, np.percentile(e, [50, 99, 100]))
-    assert np.all(e <= 64), (name, float(e.max()))
+    ref = orc.apply_many(g, P, 0, pts)
+    ok = np.all(np.isfinite(ref[:, :2]), axis=1) & (np.abs(ref[:, :2]).max(axis=1) < 1e6)
+    scale = np.maximum(np.abs(ref[:, 0]), np.abs(ref[:, 1]))
+    ulp = np.spacing(np.maximum(scale, 1e-30).astype(np.float32)).astype(np.float64)
+    fwd = np.max(np.abs(out[:, :2] - ref[:, :2]), axis=1) / ulp
+    # backward: nearest FP64 result over inputs perturbed by up to 2 ulps per coordinate
+    best = fwd.copy()
+    sx = np.spacing(pts[:, 0]).astype(np.float64)
+    sy = np.spacing(pts[:, 1]).astype(np.float64)
+    for i in range(-2, 3):
+        for j in range(-2, 3):
+            q = pts.astype(np.float64).copy()
+            q[:, 0] += i * sx
+            q[:, 1] += j * sy
+            r2 = orc.apply_many(g, P, 0, q)
+            best = np.minimum(best, np.max(np.abs(out[:, :2] - r2[:, :2]), axis=1) / ulp)
+    print(name, "forward ulp p50/p90/p99/max", np.percentile(fwd[ok], [50, 90, 99, 100]).round(2),
+          "backward max", float(best[ok].max()))
+    assert np.all(best[ok] <= 4), (name, float(best[ok].max()))
+    assert np.median(fwd[ok]) <= 1.0 and np.mean(fwd[ok] <= 4) >= 0.9, (name, np.percentile(fwd[ok], [50, 90]))
     np.testing.assert_allclose(out[:, 2], ref[:, 2], rtol=1e-6, atol=1e-7)  # colour blend
     assert np.all(out[:, 3] == 1.0)
 
@@ -205,27 +224,31 @@ def _density(hist):
     return d / d.sum()
 
 
-def _gpu_jitters(st, g, w, h):
-    """Screen offsets the device drew per temporal sample (one per block)."""
-    p_ref, _ = orc.prepared(g, w, h)
-    s = st.samples()
-    return np.stack([s[:, 4] - p_ref[4], s[:, 5] - p_ref[5]], 1)
-
-
 def _render_parity(db, comp, g, w, h, spps, channels=(3,), threads=8):
+    """GPU render vs two FP64 oracle renders fed with the same inputs: the
+    device-prepared flame parameters and 8-bit palette (interpolation parity
+    is tested on its own), the device's per-block screen jitters, and the same
+    schedule - as many chains, Hammersley start points, 20 warm-up passes and
+    the same number of drawing passes per chain."""
     f = lr.flame.from_json(db, g)
     k = comp.get_flame_kernel(db, f)
+    R = f.size_reals()
+    p_ref, _ = orc.prepared(g, w, h)
     res = {}
     for spp in spps:
         st = k.warmup(f.pack_samples(4, w, h), (w, h), seed=5, count=20)
         r = k.bin(st, lr.bailout_args(iters=0, millis=0, quality=spp))
         gpu = st.bins().cpu().numpy().astype(np.float64)
-        jit = _gpu_jitters(st, g, w, h)
-        eff = max(r.draw_count / max(r.total_passes, 1), 0.02)
-        chains = 32768
-        passes = int(r.quality * w * h / chains / eff) + 1
-        o1, _ = orc.render(g, w, h, chains, passes, seed=1, threads=threads, jitter=jit)
-        o2, _ = orc.render(g, w, h, chains, passes, seed=2, threads=threads, jitter=jit)
+        samp = st.samples()
+        params = samp[0, :R].astype(np.float64)
+        params[4], params[5] = p_ref[4], p_ref[5]
+        jit = np.stack([samp[:, 4] - p_ref[4], samp[:, 5] - p_ref[5]], 1)
+        pal = samp[0, k.info["sample_floats"] - 1024:].reshape(256, 4)[:, :3].astype(np.float64)
+        chains = k.info["grid"] * k.info["block"] * k.info["chains_per_thread"]
+        passes = max(1, int(round(r.total_passes / chains)))
+        kw = dict(warmup=20, threads=threads, params=params, palette=pal, jitter=jit, hammersley=True)
+        o1, _ = orc.render(g, w, h, chains, passes, seed=1, **kw)
+        o2, _ = orc.render(g, w, h, chains, passes, seed=2, **kw)
         for c in channels:
             a = gpu[..., c] / gpu[..., c].sum()
             b1 = o1[..., c] / o1[..., c].sum()
