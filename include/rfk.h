@@ -85,7 +85,8 @@ typedef struct {
     int precise_math;      /* 0: -use_fast_math as the reference (flame_compiler.cpp:861); 1: full-precision libm */
     int block;             /* threads per block (0 = 256) */
     int chains_per_thread; /* 0 = 4 when sorting, else 1 */
-    int flush;             /* histogram update: 0 = red.global.add.v4.f32 per draw, 1 = warp-aggregated */
+    int flush;             /* histogram update: 0 = red.global.add.v4.f32 per draw, 1 = warp-aggregated,
+                              2 = warp-aggregated into a per-block shared-memory cache of hot pixels */
     int blocks_per_sm;     /* 0 = as many as fit */
     int sort;              /* 0 = sort each warp's chains by xform when 2..32 xforms; -1 = never */
 } rfk_compile_opts;

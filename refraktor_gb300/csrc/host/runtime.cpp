@@ -234,7 +234,7 @@ void check_options(const rfk_compile_opts& o) {
     const int block = o.block > 0 ? o.block : 256;
     if (block % 32 != 0 || block > 1024) fail(RFK_E_INVALID, "block must be a multiple of 32 up to 1024");
     if (o.chains_per_thread > 8 || o.chains_per_thread < 0) fail(RFK_E_INVALID, "chains_per_thread must be in [0, 8]");
-    if (o.flush < 0 || o.flush > 1) fail(RFK_E_INVALID, "flush must be 0 or 1");
+    if (o.flush < 0 || o.flush > 2) fail(RFK_E_INVALID, "flush must be 0, 1 or 2");
     if (o.blocks_per_sm < 0) fail(RFK_E_INVALID, "negative option");
 }
 

@@ -301,8 +301,48 @@ __device__ __forceinline__ void rfk_sort_chains(float (&x)[RFK_CPT], float (&y)[
 }
 #endif
 
-__device__ __forceinline__ void rfk_flush(float4* __restrict__ bins, int idx, float4 v) {
-#if RFK_FLUSH == 1
+#if RFK_FLUSH == 2
+// Shared-memory cache of hot pixels (one per block): direct-mapped slots keyed
+// by pixel index, claimed with atomicCAS while empty and never evicted until
+// the next flush, so adds into a claimed slot never race with its flush.
+#define RFK_CACHE_SLOTS 1024
+#define RFK_CACHE_EMPTY 0xFFFFFFFFu
+struct rfk_cache {
+    unsigned tag[RFK_CACHE_SLOTS];
+    float val[4][RFK_CACHE_SLOTS];
+};
+
+__device__ __forceinline__ unsigned rfk_cache_slot(int idx) {
+    return ((unsigned)idx * 2654435761u) >> (32 - 10);
+}
+
+__device__ __forceinline__ void rfk_cache_clear(rfk_cache& cc) {
+    for (unsigned i = threadIdx.x; i < RFK_CACHE_SLOTS; i += RFK_BLOCK) {
+        cc.tag[i] = RFK_CACHE_EMPTY;
+        cc.val[0][i] = cc.val[1][i] = cc.val[2][i] = cc.val[3][i] = 0.0f;
+    }
+}
+
+// All threads of the block, between barriers: every claimed slot goes out as
+// one red.global.add.v4.f32 and the slot is emptied.
+__device__ __forceinline__ void rfk_cache_flush(rfk_cache& cc, float4* __restrict__ bins) {
+    for (unsigned i = threadIdx.x; i < RFK_CACHE_SLOTS; i += RFK_BLOCK) {
+        const unsigned t = cc.tag[i];
+        if (t != RFK_CACHE_EMPTY) {
+            rfk_red_v4(bins + t, cc.val[0][i], cc.val[1][i], cc.val[2][i], cc.val[3][i]);
+            cc.tag[i] = RFK_CACHE_EMPTY;
+            cc.val[0][i] = cc.val[1][i] = cc.val[2][i] = cc.val[3][i] = 0.0f;
+        }
+    }
+}
+#endif
+
+__device__ __forceinline__ void rfk_flush(float4* __restrict__ bins, int idx, float4 v
+#if RFK_FLUSH == 2
+                                          , rfk_cache& cc
+#endif
+) {
+#if RFK_FLUSH >= 1
     // lanes that hit the same pixel add their contributions first
     const unsigned active = __activemask();
     const unsigned same = __match_any_sync(active, idx);
@@ -321,7 +361,26 @@ __device__ __forceinline__ void rfk_flush(float4* __restrict__ bins, int idx, fl
             o.w = __shfl_sync(same, v.w, src);
             acc.x += o.x; acc.y += o.y; acc.z += o.z; acc.w += o.w;
         }
-        if ((int)lane == leader) rfk_red_v4(bins + idx, acc.x, acc.y, acc.z, acc.w);
+        if ((int)lane == leader) {
+#if RFK_FLUSH == 2
+            const unsigned slot = rfk_cache_slot(idx);
+            unsigned t = cc.tag[slot];
+            if (t == RFK_CACHE_EMPTY) {
+                t = atomicCAS(&cc.tag[slot], RFK_CACHE_EMPTY, (unsigned)idx);
+                if (t == RFK_CACHE_EMPTY) t = (unsigned)idx;
+            }
+            if (t == (unsigned)idx) {
+                atomicAdd(&cc.val[0][slot], acc.x);
+                atomicAdd(&cc.val[1][slot], acc.y);
+                atomicAdd(&cc.val[2][slot], acc.z);
+                atomicAdd(&cc.val[3][slot], acc.w);
+            } else {
+                rfk_red_v4(bins + idx, acc.x, acc.y, acc.z, acc.w);
+            }
+#else
+            rfk_red_v4(bins + idx, acc.x, acc.y, acc.z, acc.w);
+#endif
+        }
     }
 #else
     if (idx >= 0) rfk_red_v4(bins + idx, v.x, v.y, v.z, v.w);
@@ -412,6 +471,13 @@ extern "C" __global__ void __launch_bounds__(RFK_BLOCK) rfk_bin(rfk_bin_args a) 
     float4* stage = s_stage[threadIdx.x >> 5];
     const unsigned lane_stream = blockIdx.x * RFK_BLOCK + threadIdx.x;
 #endif
+#if RFK_FLUSH == 2
+    __shared__ rfk_cache cache;
+    rfk_cache_clear(cache);
+#define RFK_CACHE_ARG , cache
+#else
+#define RFK_CACHE_ARG
+#endif
     const float* src = a.samples + (size_t)blockIdx.x * RFK_SAMPLE_FLOATS;
     for (unsigned i = threadIdx.x; i < RFK_SAMPLE_FLOATS; i += RFK_BLOCK) P[i] = src[i];
     if (threadIdx.x == 0) {
@@ -462,7 +528,7 @@ extern "C" __global__ void __launch_bounds__(RFK_BLOCK) rfk_bin(rfk_bin_args a) 
                 float4 v;
                 unsigned hit;
                 int idx = rfk_move(kk[k], x[k], y[k], c[k], rng, P, a.w, a.h, v, hit);
-                rfk_flush(a.bins, idx, v);
+                rfk_flush(a.bins, idx, v RFK_CACHE_ARG);
                 my_hits += hit;
                 my_draws += (idx >= 0) ? 1u : 0u;
             }
@@ -474,7 +540,7 @@ extern "C" __global__ void __launch_bounds__(RFK_BLOCK) rfk_bin(rfk_bin_args a) 
                 float4 v;
                 unsigned hit;
                 int idx = rfk_step(x[k], y[k], c[k], last[k], rng, P, a.w, a.h, v, hit);
-                rfk_flush(a.bins, idx, v);
+                rfk_flush(a.bins, idx, v RFK_CACHE_ARG);
                 my_hits += hit;
                 my_draws += (idx >= 0) ? 1u : 0u;
             }
@@ -491,6 +557,9 @@ extern "C" __global__ void __launch_bounds__(RFK_BLOCK) rfk_bin(rfk_bin_args a) 
             atomicAdd(&s_draws, (unsigned long long)wd);
         }
         __syncthreads();
+#if RFK_FLUSH == 2
+        rfk_cache_flush(cache, a.bins);
+#endif
         if (threadIdx.x == 0) {
             unsigned long long q = atomicAdd(&a.counters->quality, s_hits) + s_hits;
             atomicAdd(&a.counters->draws, s_draws);

@@ -88,24 +88,31 @@ def _quantile_box(dens: np.ndarray, g: dict, rw: int, rh: int, q: float = 0.01):
     return to_x(x0), to_x(x1 + 1), to_y(y0), to_y(y1 + 1)
 
 
-def frame_on_gpu(db, genome: dict, w: int, h: int, seed: int = 0) -> dict:
+def frame_on_gpu(db, genome: dict, w: int, h: int, seed: int = 0, with_coverage: bool = False):
     """Refits centre and scale so that the 1%..99% box of the drawn points
     (after the final xform) fills the image: a wide low-resolution render on
-    the GPU locates the attractor, a second one at the located box refines it."""
+    the GPU locates the attractor, a second one at the located box refines it.
+    With `with_coverage`, also returns the lit fraction of a third render at
+    the final framing."""
     from . import librefrakt as lr
 
     rw = 256
     rh = max(16, int(round(rw * h / w)))
     g = dict(genome, center_x=0.0, center_y=0.0, scale=1.0 / 40.0)  # view spans 40 units vertically
     comp = lr.flame_compiler()
-    for _ in range(2):
+    coverage = 0.0
+    for it in range(3 if with_coverage else 2):
         f = lr.flame.from_json(db, g)
         k = comp.get_flame_kernel(db, f)
         st = k.warmup(f.pack_samples(4, rw, rh), (rw, rh), seed, 64)
         k.bin(st, lr.bailout_args(iters=0, millis=2000, quality=16.0))
-        box = _quantile_box(st.bins()[..., 3].double().cpu().numpy(), g, rw, rh)
+        dens = st.bins()[..., 3].double().cpu().numpy()
+        if it == 2:
+            coverage = float((dens > 0).mean())
+            break
+        box = _quantile_box(dens, g, rw, rh)
         if box is None:
-            return dict(genome)
+            return (dict(genome), 0.0) if with_coverage else dict(genome)
         x0, x1, y0, y1 = box
         span_x, span_y = max(x1 - x0, 1e-4), max(y1 - y0, 1e-4)
         # screen = (p - centre) * scale * h + (w/2, h/2): fit both extents, 5% margin
@@ -113,7 +120,23 @@ def frame_on_gpu(db, genome: dict, w: int, h: int, seed: int = 0) -> dict:
                  scale=float(min(rw / (span_x * rh), 1.0 / span_y) * 0.95))
     out = dict(genome, center_x=g["center_x"], center_y=g["center_y"],
                scale=float(g["scale"]) * (rh / rw) / (h / w))
-    return out
+    return (out, coverage) if with_coverage else out
+
+
+def visible_flame(db, make, seed: int, w: int, h: int, min_coverage: float = 0.25, tries: int = 64) -> dict:
+    """First genome make(seed * 1000 + j), j = 0, 1, ..., whose framed render
+    lights at least `min_coverage` of a 256-pixel-wide preview: the visibility
+    rejection that random flame generators apply (flam3-genome rejects
+    candidates whose test render is mostly empty), so that benchmark genomes
+    are images rather than a few collapsed points."""
+    best = None
+    for j in range(tries):
+        g, cov = frame_on_gpu(db, make(seed * 1000 + j), w, h, seed=j, with_coverage=True)
+        if cov >= min_coverage:
+            return dict(g, name=f"seed{seed}.{j}")
+        if best is None or cov > best[1]:
+            best = (g, cov, j)
+    return dict(best[0], name=f"seed{seed}.{best[2]}")
 
 
 def _base(rng: np.random.Generator, gamma: float, brightness: float) -> dict:
