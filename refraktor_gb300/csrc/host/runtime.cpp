@@ -194,7 +194,10 @@ std::vector<char> nvrtc_build(const std::string& source, const std::string& arch
     const std::string d_sort = "-DRFK_SORT=" + std::to_string(sort);
     std::vector<const char*> opts = {arch.c_str(), "-std=c++17", "-lineinfo", d_block.c_str(), d_cpt.c_str(),
                                      d_flush.c_str(), d_sort.c_str(), "-extra-device-vectorization"};
-    if (!o.precise_math) opts.push_back("--use_fast_math");
+    if (!o.precise_math) {
+        opts.push_back("--use_fast_math");
+        opts.push_back("-DRFK_FAST_HYPOT=1");
+    }
     nvrtcProgram prog;
     if (nvrtcCreateProgram(&prog, source.c_str(), "rfk_flame.cu", 0, nullptr, nullptr) != NVRTC_SUCCESS)
         fail(RFK_E_COMPILE, "nvrtcCreateProgram failed");

@@ -114,7 +114,13 @@ RFK_FN int fl_trunc(R a) { return sizeof(R) == 4 ? (int)truncf((float)a) : (int)
 RFK_FN int fl_rint(R a) { return sizeof(R) == 4 ? (int)rintf((float)a) : (int)rint((double)a); }
 RFK_FN R fl_pow(R a, R b) { return sizeof(R) == 4 ? (R)powf((float)a, (float)b) : (R)pow((double)a, (double)b); }
 RFK_FN R fl_atan2(R a, R b) { return sizeof(R) == 4 ? (R)atan2f((float)a, (float)b) : (R)atan2((double)a, (double)b); }
+#ifdef RFK_FAST_HYPOT
+// fast build: sqrt(a^2 + b^2) without hypot's overflow scaling; chain
+// positions beyond 1e10 are reset before they can square to overflow
+RFK_FN R fl_hypot(R a, R b) { return sizeof(R) == 4 ? (R)sqrtf(fmaf((float)a, (float)a, (float)b * (float)b)) : (R)hypot((double)a, (double)b); }
+#else
 RFK_FN R fl_hypot(R a, R b) { return sizeof(R) == 4 ? (R)hypotf((float)a, (float)b) : (R)hypot((double)a, (double)b); }
+#endif
 RFK_FN R fl_modf(R a, R b) { return sizeof(R) == 4 ? (R)fmodf((float)a, (float)b) : (R)fmod((double)a, (double)b); }
 RFK_FN R fl_copysign(R a, R b) { return sizeof(R) == 4 ? (R)copysignf((float)a, (float)b) : (R)copysign((double)a, (double)b); }
 RFK_FN R fl_fma(R a, R b, R c) { return sizeof(R) == 4 ? (R)fmaf((float)a, (float)b, (float)c) : (R)fma((double)a, (double)b, (double)c); }

@@ -268,26 +268,41 @@ __device__ __forceinline__ int rfk_step(float& x, float& y, float& c, unsigned& 
 // Counting sort of a warp's 32 * RFK_CPT chains by their picked xform,
 // through the warp's stage buffer in shared memory: afterwards round q of
 // every lane holds sorted slot q * 32 + lane, so the lanes of one round run
-// the same xform except at the boundaries between xform runs. Ranks come from
-// one ballot per (xform, round); only __syncwarp is needed.
+// the same xform except at the boundaries between xform runs. Each round's
+// lanes with equal xform are grouped by __match_any_sync; the group leader
+// reserves the group's places in the per-warp xform counters; a warp scan of
+// the counters gives each xform's start. Only __syncwarp is needed.
 __device__ __forceinline__ void rfk_sort_chains(float (&x)[RFK_CPT], float (&y)[RFK_CPT], float (&c)[RFK_CPT],
-                                                int (&k)[RFK_CPT], float4* __restrict__ stage) {
+                                                int (&k)[RFK_CPT], float4* __restrict__ stage,
+                                                unsigned* __restrict__ counts) {
     const unsigned lane = threadIdx.x & 31u;
     const unsigned lt = (1u << lane) - 1u;
-    unsigned pos[RFK_CPT];
-    unsigned base = 0;
+    if (lane < RFK_NX) counts[lane] = 0u;
+    __syncwarp();
+    unsigned off[RFK_CPT];
 #pragma unroll
-    for (int j = 0; j < RFK_NX; j++) {
-#pragma unroll
-        for (int q = 0; q < RFK_CPT; q++) {
-            const bool mine = (k[q] == j);
-            const unsigned b = __ballot_sync(0xffffffffu, mine);
-            if (mine) pos[q] = base + __popc(b & lt);
-            base += __popc(b);
-        }
+    for (int q = 0; q < RFK_CPT; q++) {
+        const unsigned same = __match_any_sync(0xffffffffu, k[q]);
+        const int leader = __ffs(same) - 1;
+        unsigned base = 0;
+        if ((int)lane == leader) base = atomicAdd(&counts[k[q]], (unsigned)__popc(same));
+        off[q] = __shfl_sync(0xffffffffu, base, leader) + __popc(same & lt);
     }
+    __syncwarp();
+    // exclusive scan of the per-xform counts across lanes 0..RFK_NX-1
+    unsigned cnt = (lane < RFK_NX) ? counts[lane] : 0u;
+    unsigned incl = cnt;
 #pragma unroll
-    for (int q = 0; q < RFK_CPT; q++) stage[pos[q]] = make_float4(x[q], y[q], c[q], __int_as_float(k[q]));
+    for (int d = 1; d < 32; d <<= 1) {
+        const unsigned v = __shfl_up_sync(0xffffffffu, incl, d);
+        if ((int)lane >= d) incl += v;
+    }
+    const unsigned start = incl - cnt;
+#pragma unroll
+    for (int q = 0; q < RFK_CPT; q++) {
+        const unsigned pos = __shfl_sync(0xffffffffu, start, k[q]) + off[q];
+        stage[pos] = make_float4(x[q], y[q], c[q], __int_as_float(k[q]));
+    }
     __syncwarp();
 #pragma unroll
     for (int q = 0; q < RFK_CPT; q++) {
@@ -461,6 +476,28 @@ struct rfk_bin_args {
     rfk_counters* counters;
 };
 
+// Rotates the per-lane chain slots by one (slot q takes slot q + 1), with
+// register moves only.
+template <typename T0, typename T1>
+__device__ __forceinline__ void rfk_rot1(T0 (&a)[RFK_CPT], T1 (&b)[RFK_CPT]) {
+    const T0 a0 = a[0];
+    const T1 b0 = b[0];
+#pragma unroll
+    for (int q = 0; q + 1 < RFK_CPT; q++) {
+        a[q] = a[q + 1];
+        b[q] = b[q + 1];
+    }
+    a[RFK_CPT - 1] = a0;
+    b[RFK_CPT - 1] = b0;
+}
+
+__device__ __forceinline__ void rfk_rotate(float (&x)[RFK_CPT], float (&y)[RFK_CPT], float (&c)[RFK_CPT], int (&k)[RFK_CPT],
+                                           unsigned (&last)[RFK_CPT], unsigned (&chain)[RFK_CPT]) {
+    rfk_rot1(x, y);
+    rfk_rot1(c, k);
+    rfk_rot1(last, chain);
+}
+
 extern "C" __global__ void __launch_bounds__(RFK_BLOCK) rfk_bin(rfk_bin_args a) {
     __shared__ __align__(16) float P[RFK_SAMPLE_FLOATS];
     __shared__ unsigned long long s_hits, s_draws;
@@ -468,7 +505,9 @@ extern "C" __global__ void __launch_bounds__(RFK_BLOCK) rfk_bin(rfk_bin_args a) 
     __shared__ unsigned long long s_start;
 #if RFK_SORT
     __shared__ float4 s_stage[RFK_BLOCK / 32][32 * RFK_CPT];
+    __shared__ unsigned s_counts[RFK_BLOCK / 32][32];
     float4* stage = s_stage[threadIdx.x >> 5];
+    unsigned* counts = s_counts[threadIdx.x >> 5];
     const unsigned lane_stream = blockIdx.x * RFK_BLOCK + threadIdx.x;
 #endif
 #if RFK_FLUSH == 2
@@ -517,20 +556,23 @@ extern "C" __global__ void __launch_bounds__(RFK_BLOCK) rfk_bin(rfk_bin_args a) 
             int kk[RFK_CPT];
 #pragma unroll
             for (int k = 0; k < RFK_CPT; k++) kk[k] = rfk_pick(pr.u01(), P, last[k]);
-            rfk_sort_chains(x, y, c, kk, stage);
-#pragma unroll
+            rfk_sort_chains(x, y, c, kk, stage, counts);
+            // One copy of the chain-step code (smaller instruction footprint):
+            // the chain in slot 0 is moved, then the slots rotate by one.
+#pragma unroll 1
             for (int k = 0; k < RFK_CPT; k++) {
 #if RFK_CHAOS
-                last[k] = (unsigned)kk[k];
+                last[0] = (unsigned)kk[0];
 #endif
                 Rng rng;
-                rng.start_lazy(chain[k], a.call_id, pass, a.seed, a.salt);
+                rng.start_lazy(chain[0], a.call_id, pass, a.seed, a.salt);
                 float4 v;
                 unsigned hit;
-                int idx = rfk_move(kk[k], x[k], y[k], c[k], rng, P, a.w, a.h, v, hit);
+                int idx = rfk_move(kk[0], x[0], y[0], c[0], rng, P, a.w, a.h, v, hit);
                 rfk_flush(a.bins, idx, v RFK_CACHE_ARG);
                 my_hits += hit;
                 my_draws += (idx >= 0) ? 1u : 0u;
+                rfk_rotate(x, y, c, kk, last, chain);
             }
 #else
 #pragma unroll
