@@ -3,8 +3,10 @@
 Workload: the plain 1080p single flame - 1920x1080, 1024 spp, 8 xforms with
 Dirichlet(1) weights plus a final xform, 1-3 variations each from the
 14-variation set, density-estimation blur (radius 0-9 px ~ 1/sqrt(density)),
-tonemap; seeded synthetic genome (synthetic.hd_flame(0), camera fitted on the
-GPU), since the reference publishes no benchmark genomes.
+tonemap. The genome is the committed seeded synthetic workload
+refraktor_gb300/workloads/hd_1080p.json (the reference publishes no benchmark
+genomes); the launch shape and histogram-flush strategy come from the
+library's autotuner.
 
 One step = one frame: bin to 1024 spp on a warmed state (value), or the full
 public-API path from host genome samples to a host image (e2e).
@@ -98,6 +100,10 @@ def _flush_l2(buf):
     buf.fill_(1.0)
 
 
+def load_workload(name: str = "hd_1080p.json") -> dict:
+    return json.loads((ROOT / "refraktor_gb300" / "workloads" / name).read_text())
+
+
 def run_gpu(args) -> dict:
     import torch
 
@@ -113,12 +119,13 @@ def run_gpu(args) -> dict:
         dist.init_process_group("nccl")
     build.build()
     db = lr.flamedb()
-    genome = syn.frame_on_gpu(db, syn.hd_flame(0), W, H)
+    genome = load_workload()
     f = lr.flame.from_json(db, genome)
     tp = f.tonemap_params()
     comp = lr.flame_compiler()
-    k = comp.get_flame_kernel(db, f)
     samples = f.pack_samples(4, W, H)
+    tuned, tune_report = lr.autotune(db, f, samples, (W, H))
+    k = comp.get_flame_kernel(db, f, **tuned)
     stream = torch.cuda.Stream()
     flush = torch.empty(512 << 20 >> 2, dtype=torch.float32, device="cuda")
 
@@ -204,10 +211,11 @@ def run_gpu(args) -> dict:
         "scaling": "weak",
         "vs_baseline": None,
         "dtype": "f32",
-        "data": "synthetic (seeded genome synthetic.hd_flame(0), camera fitted on the GPU)",
-        "config": {"workload": WORKLOAD, "width": W, "height": H, "spp": SPP, "xforms": 8, "final_xform": True,
-                   "grid": info["grid"], "block": info["block"], "chains_per_thread": info["chains_per_thread"],
-                   "flush": info["flush"], "l2": "512 MiB buffer written between timed steps",
+        "data": "synthetic (seeded genome refraktor_gb300/workloads/hd_1080p.json)",
+        "config": {"workload": WORKLOAD, "genome": genome.get("name"), "width": W, "height": H, "spp": SPP, "xforms": 8,
+                   "final_xform": True, "grid": info["grid"], "block": info["block"],
+                   "chains_per_thread": info["chains_per_thread"], "flush": info["flush"], "sort": info["sort"],
+                   "autotune": tune_report, "l2": "512 MiB buffer written between timed steps",
                    "parallelism": f"replicas x{ws}"},
         "e2e": {"value": e2e_passes / e2e_t, "unit": "iterations/s", "s_per_frame": e2e_t / args.steps,
                 "h2d_bytes_per_step": int(samples.nbytes), "d2h_bytes_per_step": int(W * H * 4 * 2)},
@@ -236,11 +244,16 @@ def cpu_baseline(genome: dict, seconds: float = 12.0, threads: int | None = None
     threads = threads or os.cpu_count() or 1
     chains = 64 * threads
     params, pal = orc.prepared(genome, W, H)
-    # calibrate passes for about `seconds` of work
-    t0 = time.perf_counter()
-    orc.render(genome, W, H, chains, 200, warmup=WARMUP_PASSES, threads=threads, params=params, palette=pal)
-    dt = time.perf_counter() - t0
-    passes = max(200, int(200 * seconds / max(dt, 1e-3)))
+    # calibrate passes for about `seconds` of work: grow a probe to >= 0.5 s
+    probe = 200
+    while True:
+        t0 = time.perf_counter()
+        orc.render(genome, W, H, chains, probe, warmup=WARMUP_PASSES, threads=threads, params=params, palette=pal)
+        dt = time.perf_counter() - t0
+        if dt >= 0.5 or probe > 1 << 26:
+            break
+        probe *= 4
+    passes = max(probe, int(probe * seconds / dt))
     t0 = time.perf_counter()
     _, draws = orc.render(genome, W, H, chains, passes, warmup=WARMUP_PASSES, threads=threads, params=params,
                           palette=pal)
@@ -257,21 +270,7 @@ def run_reference(args) -> dict:
     ws, rank = _dist()
     if rank != 0:
         return {}
-    from refraktor_gb300 import synthetic as syn
-
-    genome = syn.hd_flame(0)
-    genome.update(center_x=0.0, center_y=0.0, scale=0.25)
-    try:
-        import torch  # noqa: F401
-
-        if torch.cuda.is_available():
-            from refraktor_gb300 import build
-            from refraktor_gb300 import librefrakt as lr
-
-            build.build()
-            genome = syn.frame_on_gpu(lr.flamedb(), syn.hd_flame(0), W, H)
-    except Exception:
-        pass
+    genome = load_workload()
     vals = []
     for _ in range(args.warmup):
         cpu_baseline(genome, seconds=2.0)

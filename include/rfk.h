@@ -236,6 +236,22 @@ rfk_status rfk_catmull_coefficients(const double* samples, uint32_t sample_size,
 rfk_status rfk_fix_rotation(double* samples, size_t nsamples, size_t sample_size, size_t flame_size,
                             const size_t* affine_indices, size_t n_affine);
 
+/* ---- autotuner --------------------------------------------------------------
+ * No reference counterpart (the reference picks its launch shape from
+ * occupancy alone, flame_compiler.cpp:807-864). Times candidate launch shapes
+ * (threads per block, chains per thread) and histogram-flush strategies on
+ * this flame at this image size - `passes` passes per chain per candidate -
+ * and returns the fastest as compile options. Results are cached per
+ * (database, structure, genome values, size); a cached answer reports
+ * candidates = 0. */
+typedef struct {
+    int candidates;
+    double best_iters_per_s;
+    double worst_iters_per_s;
+} rfk_tune_report;
+rfk_status rfk_autotune(const rfk_db* db, const rfk_flame* f, const double* samples, size_t nsamples, uint32_t w, uint32_t h,
+                        uint32_t passes, rfk_compile_opts* best, rfk_tune_report* report);
+
 /* ---- measurement helpers -------------------------------------------------- */
 /* red.global.add.v4.f32 operations per second into a device buffer of
  * `bytes` (random slots): the L2-atomic roofline. */

@@ -38,6 +38,10 @@ class BinResult(C.Structure):
         return {k: getattr(self, k) for k, _ in self._fields_}
 
 
+class TuneReport(C.Structure):
+    _fields_ = [("candidates", C.c_int), ("best_iters_per_s", C.c_double), ("worst_iters_per_s", C.c_double)]
+
+
 class TonemapArgs(C.Structure):
     _fields_ = [("quality", C.c_double), ("gamma", C.c_double), ("brightness", C.c_double), ("vibrancy", C.c_double),
                 ("max_density", C.c_double), ("highlight_power", C.c_double), ("precise", C.c_int)]
@@ -94,6 +98,8 @@ SIGNATURES = {
     "rfk_fix_rotation": (C.c_int, [C.c_void_p, C.c_size_t, C.c_size_t, C.c_size_t, C.c_void_p, C.c_size_t]),
     "rfk_probe_red_v4": (C.c_int, [C.c_size_t, C.c_uint32, C.POINTER(C.c_double)]),
     "rfk_device_sm_count": (C.c_int, []),
+    "rfk_autotune": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_size_t, C.c_uint32, C.c_uint32, C.c_uint32,
+                               C.POINTER(CompileOpts), C.POINTER(TuneReport)]),
 }
 
 

@@ -853,6 +853,83 @@ rfk_status rfk_probe_red_v4(size_t bytes, uint32_t iters, double* ops_per_s) {
     });
 }
 
+// ---------------------------------------------------------------- autotune --
+// Times candidate launch shapes and histogram-flush strategies on the flame
+// itself (the best choice depends on how concentrated its draws are), and
+// keeps the fastest per (database, structure, genome values, image size).
+namespace {
+std::mutex g_tune_mu;
+std::map<std::string, std::pair<rfk_compile_opts, double>> g_tune_cache;
+}  // namespace
+
+rfk_status rfk_autotune(const rfk_db* db, const rfk_flame* f, const double* samples, size_t nsamples, uint32_t w, uint32_t h,
+                        uint32_t passes, rfk_compile_opts* best, rfk_tune_report* report) {
+    return guard([&] {
+        if (!db || !f || !samples || !best) fail(RFK_E_INVALID, "null argument");
+        if (passes == 0) passes = 32;
+        const size_t ss = f->f.size_reals() + rfk::palette_reals;
+        std::ostringstream key;
+        key << db->db.hash() << "|" << f->f.structure_key() << "|" << w << "x" << h << "|" << passes << "|";
+        uint64_t vh = 1469598103934665603ull;
+        const unsigned char* bytes = reinterpret_cast<const unsigned char*>(samples);
+        for (size_t i = 0; i < nsamples * ss * sizeof(double); i++) vh = (vh ^ bytes[i]) * 1099511628211ull;
+        key << vh;
+        {
+            std::lock_guard<std::mutex> lk(g_tune_mu);
+            auto it = g_tune_cache.find(key.str());
+            if (it != g_tune_cache.end()) {
+                *best = it->second.first;
+                if (report) {
+                    report->candidates = 0;
+                    report->best_iters_per_s = it->second.second;
+                    report->worst_iters_per_s = it->second.second;
+                }
+                return;
+            }
+        }
+        struct cand { int block, cpt, flush; };
+        const cand cands[] = {{256, 4, 0}, {256, 4, 1}, {256, 4, 2}, {128, 4, 0}, {128, 4, 1}, {512, 4, 1}};
+        double best_rate = -1.0, worst_rate = 1e300;
+        int n = 0;
+        for (const cand& c : cands) {
+            rfk_compile_opts o{};
+            o.block = c.block;
+            o.chains_per_thread = c.cpt;
+            o.flush = c.flush;
+            rfk_kernel* kh = nullptr;
+            if (rfk_compile(db, f, &o, &kh, nullptr, 0) != RFK_OK) continue;
+            rfk_state* st = nullptr;
+            rfk_status ws = rfk_warmup(kh, samples, nsamples, w, h, 1, 20, 1, nullptr, &st);
+            if (ws != RFK_OK) {
+                rfk_kernel_destroy(kh);
+                continue;
+            }
+            rfk_bailout bo{passes, 0, 0.0};
+            rfk_bin_result r{};
+            double rate = 0.0;
+            if (rfk_bin(st, &bo, nullptr, &r) == RFK_OK && rfk_bin(st, &bo, nullptr, &r) == RFK_OK && r.elapsed_ms > 0)
+                rate = (double)r.total_passes / (r.elapsed_ms * 1e-3);
+            rfk_state_destroy(st);
+            rfk_kernel_destroy(kh);
+            if (rate <= 0) continue;
+            n++;
+            worst_rate = std::min(worst_rate, rate);
+            if (rate > best_rate) {
+                best_rate = rate;
+                *best = o;
+            }
+        }
+        if (n == 0) fail(RFK_E_CUDA, "no autotune candidate ran");
+        if (report) {
+            report->candidates = n;
+            report->best_iters_per_s = best_rate;
+            report->worst_iters_per_s = worst_rate;
+        }
+        std::lock_guard<std::mutex> lk(g_tune_mu);
+        g_tune_cache[key.str()] = {*best, best_rate};
+    });
+}
+
 int rfk_device_sm_count(void) {
     int n = 0;
     rfk_status s = guard([&] { n = device_sm_count(); });

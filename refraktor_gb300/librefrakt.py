@@ -21,7 +21,7 @@ from typing import Optional, Sequence
 import numpy as np
 
 from . import _lib
-from ._lib import Bailout, BinResult, CompileOpts, DEArgs, KernelInfo, RfkError, TonemapArgs, check, lib, text_out
+from ._lib import Bailout, BinResult, CompileOpts, DEArgs, KernelInfo, RfkError, TonemapArgs, TuneReport, check, lib, text_out
 
 DEFAULT_CONFIG = Path(__file__).resolve().parent / "config"
 
@@ -305,6 +305,18 @@ class flame_compiler:
         k = flame_kernel(h)
         k.log = log.value.decode()
         return k
+
+
+def autotune(db: flamedb, f: flame, samples: np.ndarray, dims: Sequence[int], passes: int = 32) -> tuple[dict, dict]:
+    """Times launch shapes and flush strategies on this flame; returns
+    (compile options, report)."""
+    s = np.ascontiguousarray(samples, dtype=np.float64)
+    o = CompileOpts()
+    rep = TuneReport()
+    check(lib().rfk_autotune(db._h, f._h, s.ctypes.data, s.size // f.sample_size(), int(dims[0]), int(dims[1]), passes,
+                             C.byref(o), C.byref(rep)))
+    opts = {k: getattr(o, k) for k, _ in CompileOpts._fields_}
+    return opts, {k: getattr(rep, k) for k, _ in TuneReport._fields_}
 
 
 class tonemapper:
