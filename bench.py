@@ -291,8 +291,35 @@ def run_reference(args) -> dict:
     }
 
 
+def run_ncu_case(args) -> None:
+    """Small case for ncu captures of rfk_bin: the 1080p workload genome,
+    warm-up, then `--ncu-launches` bin launches to 16 spp each (~1 ms), with
+    the autotuned options unless --flush/--cpt/--block are given."""
+    from refraktor_gb300 import build
+    from refraktor_gb300 import librefrakt as lr
+
+    build.build()
+    db = lr.flamedb()
+    f = lr.flame.from_json(db, load_workload())
+    samples = f.pack_samples(4, W, H)
+    if args.flush is None:
+        opts, _ = lr.autotune(db, f, samples, (W, H))
+    else:
+        opts = dict(flush=args.flush, chains_per_thread=args.cpt, block=args.block)
+    k = lr.flame_compiler().get_flame_kernel(db, f, **opts)
+    st = k.warmup(samples, (W, H), 1, WARMUP_PASSES)
+    for _ in range(args.ncu_launches):
+        r = k.bin(st, lr.bailout_args(iters=0, millis=0, quality=16.0))
+    print(json.dumps({"ncu_case": k.info, "opts": opts, "passes": r.total_passes, "ms": r.elapsed_ms}))
+
+
 def main():
     ap = argparse.ArgumentParser()
+    ap.add_argument("--ncu-case", action="store_true")
+    ap.add_argument("--ncu-launches", type=int, default=2)
+    ap.add_argument("--flush", type=int, default=None)
+    ap.add_argument("--cpt", type=int, default=4)
+    ap.add_argument("--block", type=int, default=256)
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
@@ -300,6 +327,9 @@ def main():
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     args = ap.parse_args()
+    if args.ncu_case:
+        run_ncu_case(args)
+        return
     line = run_reference(args) if args.impl == "reference" else run_gpu(args)
     if line:
         print(json.dumps(line))
