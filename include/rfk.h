@@ -182,6 +182,22 @@ rfk_status rfk_apply_xform(const rfk_kernel* k, const float* params, int xform, 
 rfk_status rfk_prepare_samples(const rfk_kernel* k, const double* samples, size_t nsamples, const uint32_t* seg,
                                const float* t, size_t count, uint32_t seed, float* out);
 
+/* Variant of rfk_prepare_samples that allocates no device memory. It has no
+ * counterpart in the reference. It is for callers that cannot call cudaMalloc
+ * while they run: applications whose device memory belongs to their own pool
+ * or that reserve it all at start, and real-time loops that must not stall on
+ * the device-wide synchronisation of cudaMalloc / cudaFree. Its device
+ * temporaries (FP64 samples, spline segments, schedule, output blocks) live
+ * in a fixed 4 MiB array that every device using the library holds until
+ * exit; requests that need more fail with RFK_E_INVALID and say how much they
+ * need. The first call on a device takes the array's device address (make it
+ * before any stream capture). Calls share the array and run on the legacy
+ * default stream, blocking until the output is on the host: calls that could
+ * overlap on the GPU (from several threads or processes) race on the array.
+ * Every region is fully written before it is read, so nothing needs clearing. */
+rfk_status rfk_prepare_samples_noalloc(const rfk_kernel* k, const double* samples, size_t nsamples, const uint32_t* seg,
+                                       const float* t, size_t count, uint32_t seed, float* out);
+
 /* ---- image steps ----------------------------------------------------------
  * tonemapper::run(bins, out, args, stream)
  *   src/librefrakt/include/librefrakt/image/tonemapper.h:10-22,

@@ -90,6 +90,8 @@ SIGNATURES = {
     "rfk_apply_xform": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int, C.c_void_p, C.c_size_t, C.c_void_p, C.c_uint32]),
     "rfk_prepare_samples": (C.c_int, [C.c_void_p, C.c_void_p, C.c_size_t, C.c_void_p, C.c_void_p, C.c_size_t, C.c_uint32,
                                       C.c_void_p]),
+    "rfk_prepare_samples_noalloc": (C.c_int, [C.c_void_p, C.c_void_p, C.c_size_t, C.c_void_p, C.c_void_p, C.c_size_t,
+                                              C.c_uint32, C.c_void_p]),
     "rfk_tonemap": (C.c_int, [C.c_void_p, C.c_uint32, C.c_uint32, C.c_void_p, C.c_int, C.POINTER(TonemapArgs), C.c_void_p,
                               C.c_void_p, C.c_void_p]),
     "rfk_density_histogram": (C.c_int, [C.c_void_p, C.c_uint32, C.c_void_p, C.c_void_p, C.c_void_p]),

@@ -769,6 +769,60 @@ rfk_status rfk_prepare_samples(const rfk_kernel* kh, const double* samples, size
     });
 }
 
+rfk_status rfk_prepare_samples_noalloc(const rfk_kernel* kh, const double* samples, size_t nsamples, const uint32_t* seg,
+                                       const float* t, size_t count, uint32_t seed, float* out) {
+    return guard([&] {
+        const kernel_impl& k = K(kh);
+        if (!samples || !seg || !t || !out) fail(RFK_E_INVALID, "null argument");
+        if (count == 0) return;
+        if (nsamples < 4) fail(RFK_E_INVALID, "need at least 4 packed samples");
+        const size_t ss = k.gen.size_reals + rfk::palette_reals;
+        const size_t nseg = nsamples - 3;
+        for (size_t i = 0; i < count; i++)
+            if (seg[i] >= nseg) fail(RFK_E_INVALID, "segment index out of range");
+        const size_t naff = k.gen.affine_indices.size();
+        unsigned aff[1024];
+        if (naff > 1024) fail(RFK_E_INVALID, "more than 1024 affines");
+        for (size_t i = 0; i < naff; i++) aff[i] = (unsigned)k.gen.affine_indices[i];
+        // scratch layout, each region 256-byte aligned
+        auto up = [](size_t b) { return (b + 255) / 256 * 256; };
+        const size_t b_samples = up(nsamples * ss * sizeof(double));
+        const size_t b_coeff = up(nseg * ss * sizeof(float4));
+        const size_t b_aff = up(naff * sizeof(unsigned));
+        const size_t b_seg = up(count * sizeof(uint32_t));
+        const size_t b_t = up(count * sizeof(float));
+        const size_t b_out = up(count * k.sample_floats * sizeof(float));
+        const size_t need = b_samples + b_coeff + b_aff + b_seg + b_t + b_out;
+        void* base = nullptr;
+        size_t cap = 0;
+        cuda_check(rfk_noalloc_scratch_address(&base, &cap), "no-alloc scratch address");
+        if (need > cap)
+            fail(RFK_E_INVALID, "request needs " + std::to_string(need) + " bytes of device scratch; the no-alloc scratch holds " +
+                                    std::to_string(cap));
+        char* p = static_cast<char*>(base);
+        double* d_samples = reinterpret_cast<double*>(p);
+        float4* d_coeff = reinterpret_cast<float4*>(p + b_samples);
+        unsigned* d_aff = reinterpret_cast<unsigned*>(p + b_samples + b_coeff);
+        unsigned* d_seg = reinterpret_cast<unsigned*>(p + b_samples + b_coeff + b_aff);
+        float* d_t = reinterpret_cast<float*>(p + b_samples + b_coeff + b_aff + b_seg);
+        float* d_out = reinterpret_cast<float*>(p + b_samples + b_coeff + b_aff + b_seg + b_t);
+        cudaStream_t s = nullptr;
+        cuda_check(cudaMemcpyAsync(d_samples, samples, nsamples * ss * sizeof(double), cudaMemcpyHostToDevice, s), "H2D samples");
+        cuda_check(cudaMemcpyAsync(d_aff, aff, naff * sizeof(unsigned), cudaMemcpyHostToDevice, s), "H2D affines");
+        cuda_check(cudaMemcpyAsync(d_seg, seg, count * sizeof(uint32_t), cudaMemcpyHostToDevice, s), "H2D schedule");
+        cuda_check(cudaMemcpyAsync(d_t, t, count * sizeof(float), cudaMemcpyHostToDevice, s), "H2D schedule");
+        cuda_check(rfk_launch_fix_rotation(d_samples, (unsigned)nsamples, (unsigned)ss, (unsigned)k.gen.size_reals, d_aff,
+                                           (unsigned)naff, s),
+                   "fix_rotation");
+        cuda_check(rfk_launch_catmull(d_samples, (unsigned)ss, (unsigned)nseg, d_coeff, s), "catmull");
+        unsigned sz = (unsigned)ss, salt = k.salt, sd = seed;
+        void* args[] = {&d_coeff, &sz, &d_seg, &d_t, &d_out, &sd, &salt};
+        launch(k.f_prepare, (unsigned)count, 256, s, args, "rfk_prepare");
+        cuda_check(cudaMemcpyAsync(out, d_out, count * k.sample_floats * sizeof(float), cudaMemcpyDeviceToHost, s), "D2H");
+        cuda_check(cudaStreamSynchronize(s), "prepare");
+    });
+}
+
 rfk_status rfk_tonemap(const float* bins, uint32_t w, uint32_t h, void* out, int format, const rfk_tonemap_args* a,
                        uint64_t* histogram, uint64_t* max_density, void* stream) {
     return guard([&] {

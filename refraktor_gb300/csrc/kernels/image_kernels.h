@@ -7,6 +7,7 @@
 #define RFK_DE_STEPS 4         // blur radius quantisation: 1/4 px
 #define RFK_DE_MAX_RADIUS_CAP 9
 #define RFK_DE_LEVELS (RFK_DE_MAX_RADIUS_CAP * RFK_DE_STEPS + 1)
+#define RFK_NOALLOC_SCRATCH_BYTES (4u << 20)  // fixed scratch of rfk_prepare_samples_noalloc
 
 #ifdef __cplusplus
 extern "C" {
@@ -23,6 +24,11 @@ cudaError_t rfk_launch_de_blur(const float4* in, float4* out, unsigned w, unsign
 cudaError_t rfk_launch_red_v4_probe(float4* buf, unsigned long long n, unsigned iters, unsigned blocks, unsigned threads,
                                     cudaStream_t s);
 cudaError_t rfk_launch_clear_counters(unsigned long long* c, cudaStream_t s);
+// noalloc.cu: device address and size of the fixed scratch array on the
+// current device (taken once per device), and the device fix_rotation.
+cudaError_t rfk_noalloc_scratch_address(void** addr, size_t* bytes);
+cudaError_t rfk_launch_fix_rotation(double* samples, unsigned n, unsigned sample_size, unsigned flame_size,
+                                    const unsigned* aff, unsigned naff, cudaStream_t s);
 
 #ifdef __cplusplus
 }
