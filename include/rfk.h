@@ -88,7 +88,8 @@ typedef struct {
     int flush;             /* histogram update: 0 = red.global.add.v4.f32 per draw, 1 = warp-aggregated,
                               2 = warp-aggregated into a per-block shared-memory cache of hot pixels */
     int blocks_per_sm;     /* 0 = as many as fit */
-    int sort;              /* 0 = sort each warp's chains by xform when 2..32 xforms; -1 = never */
+    int sort;              /* 0 or 1 = sort each warp's chains by xform every pass, 2 = sort the whole
+                              block's chains (both when 2..32 xforms); -1 = never */
 } rfk_compile_opts;
 
 typedef struct {
@@ -96,7 +97,7 @@ typedef struct {
     int block;
     int chains_per_thread;
     int flush;
-    int sort;               /* 1 when chains are sorted by xform every pass */
+    int sort;               /* 1 / 2 when chains are sorted by xform every pass (warp / block) */
     int registers;          /* of the bin kernel */
     int num_xforms;
     int has_final;

@@ -224,8 +224,8 @@ std::vector<char> nvrtc_build(const std::string& source, const std::string& arch
 // per-xform ballots stay few (sort = 0 in the options means this choice).
 int resolve_sort(const rfk_compile_opts& o, size_t nx) {
     const bool can = nx >= 2 && nx <= 32;
-    if (o.sort < 0) return 0;
-    return can ? 1 : 0;
+    if (o.sort < 0 || !can) return 0;
+    return o.sort == 2 ? 2 : 1;
 }
 
 int resolve_cpt(const rfk_compile_opts& o, int sort) {
@@ -941,8 +941,9 @@ rfk_status rfk_autotune(const rfk_db* db, const rfk_flame* f, const double* samp
                 return;
             }
         }
-        struct cand { int block, cpt, flush; };
-        const cand cands[] = {{256, 4, 0}, {256, 4, 1}, {256, 4, 2}, {128, 4, 0}, {128, 4, 1}, {512, 4, 1}};
+        struct cand { int block, cpt, flush, sort; };
+        const cand cands[] = {{256, 4, 0, 1}, {256, 4, 1, 1}, {256, 4, 2, 1}, {128, 4, 1, 1},
+                              {256, 4, 0, 2}, {256, 4, 1, 2}, {256, 4, 2, 2}, {512, 2, 1, 2}};
         double best_rate = -1.0, worst_rate = 1e300;
         int n = 0;
         for (const cand& c : cands) {
@@ -950,6 +951,7 @@ rfk_status rfk_autotune(const rfk_db* db, const rfk_flame* f, const double* samp
             o.block = c.block;
             o.chains_per_thread = c.cpt;
             o.flush = c.flush;
+            o.sort = c.sort;
             rfk_kernel* kh = nullptr;
             if (rfk_compile(db, f, &o, &kh, nullptr, 0) != RFK_OK) continue;
             rfk_state* st = nullptr;

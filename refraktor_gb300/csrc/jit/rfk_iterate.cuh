@@ -314,6 +314,74 @@ __device__ __forceinline__ void rfk_sort_chains(float (&x)[RFK_CPT], float (&y)[
     }
     __syncwarp();
 }
+
+#define RFK_NW (RFK_BLOCK / 32)
+// Block-wide counting sort of the block's RFK_BLOCK * RFK_CPT chains by picked
+// xform (deterministic order: xform-major, then warp, then round, then lane).
+// counts[RFK_NX * RFK_NW] must be zero on entry; it is used in place for the
+// starts. `next` (the other counter set) is cleared between the first and the
+// second barrier: every thread finished the previous pass's reads of it before
+// the first barrier, and every thread's next-pass updates of it come after the
+// second. Afterwards thread t holds sorted slots q * RFK_BLOCK + t, so a warp's
+// round covers 32 consecutive slots of one xform run except at run ends.
+__device__ __forceinline__ void rfk_block_sort(float (&x)[RFK_CPT], float (&y)[RFK_CPT], float (&c)[RFK_CPT],
+                                               int (&k)[RFK_CPT], float4* __restrict__ stage,
+                                               unsigned* __restrict__ counts, unsigned* __restrict__ next) {
+    const unsigned lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
+    const unsigned lt = (1u << lane) - 1u;
+    unsigned off[RFK_CPT];
+#pragma unroll
+    for (int q = 0; q < RFK_CPT; q++) {
+        const unsigned same = __match_any_sync(0xffffffffu, k[q]);
+        const int leader = __ffs(same) - 1;
+        unsigned base = 0;
+        if ((int)lane == leader) base = atomicAdd(&counts[k[q] * RFK_NW + warp], (unsigned)__popc(same));
+        off[q] = __shfl_sync(0xffffffffu, base, leader) + __popc(same & lt);
+    }
+    __syncthreads();
+    for (unsigned i = threadIdx.x; i < RFK_NX * RFK_NW; i += RFK_BLOCK) next[i] = 0u;
+    if (warp == 0) {
+        // exclusive scan of counts[] (xform-major) by one warp
+        constexpr unsigned N = RFK_NX * RFK_NW;
+        constexpr unsigned E = (N + 31) / 32;
+        unsigned local[E];
+        unsigned sum = 0;
+#pragma unroll
+        for (unsigned e = 0; e < E; e++) {
+            const unsigned i = lane * E + e;
+            local[e] = (i < N) ? counts[i] : 0u;
+            sum += local[e];
+        }
+        unsigned incl = sum;
+#pragma unroll
+        for (int d = 1; d < 32; d <<= 1) {
+            const unsigned v = __shfl_up_sync(0xffffffffu, incl, d);
+            if ((int)lane >= d) incl += v;
+        }
+        unsigned run = incl - sum;
+#pragma unroll
+        for (unsigned e = 0; e < E; e++) {
+            const unsigned i = lane * E + e;
+            if (i < N) counts[i] = run;
+            run += local[e];
+        }
+    }
+    __syncthreads();
+#pragma unroll
+    for (int q = 0; q < RFK_CPT; q++) {
+        const unsigned pos = counts[k[q] * RFK_NW + warp] + off[q];
+        stage[pos] = make_float4(x[q], y[q], c[q], __int_as_float(k[q]));
+    }
+    __syncthreads();
+#pragma unroll
+    for (int q = 0; q < RFK_CPT; q++) {
+        const float4 v = stage[q * RFK_BLOCK + threadIdx.x];
+        x[q] = v.x;
+        y[q] = v.y;
+        c[q] = v.z;
+        k[q] = __float_as_int(v.w);
+    }
+}
 #endif
 
 #if RFK_FLUSH == 2
@@ -503,11 +571,17 @@ extern "C" __global__ void __launch_bounds__(RFK_BLOCK) rfk_bin(rfk_bin_args a) 
     __shared__ unsigned long long s_hits, s_draws;
     __shared__ unsigned s_bail;
     __shared__ unsigned long long s_start;
-#if RFK_SORT
+#if RFK_SORT == 1
     __shared__ float4 s_stage[RFK_BLOCK / 32][32 * RFK_CPT];
     __shared__ unsigned s_counts[RFK_BLOCK / 32][32];
     float4* stage = s_stage[threadIdx.x >> 5];
     unsigned* counts = s_counts[threadIdx.x >> 5];
+#elif RFK_SORT == 2
+    __shared__ float4 s_stage[RFK_BLOCK * RFK_CPT];
+    __shared__ unsigned s_counts[2][RFK_NX * (RFK_BLOCK / 32)];
+    for (unsigned i = threadIdx.x; i < 2 * RFK_NX * (RFK_BLOCK / 32); i += RFK_BLOCK) (&s_counts[0][0])[i] = 0u;
+#endif
+#if RFK_SORT
     const unsigned lane_stream = blockIdx.x * RFK_BLOCK + threadIdx.x;
 #endif
 #if RFK_FLUSH == 2
@@ -556,7 +630,12 @@ extern "C" __global__ void __launch_bounds__(RFK_BLOCK) rfk_bin(rfk_bin_args a) 
             int kk[RFK_CPT];
 #pragma unroll
             for (int k = 0; k < RFK_CPT; k++) kk[k] = rfk_pick(pr.u01(), P, last[k]);
+#if RFK_SORT == 2
+            // ping-pong counter sets, one per pass parity
+            rfk_block_sort(x, y, c, kk, s_stage, s_counts[pass & 1], s_counts[(pass + 1) & 1]);
+#else
             rfk_sort_chains(x, y, c, kk, stage, counts);
+#endif
             // One copy of the chain-step code (smaller instruction footprint):
             // the chain in slot 0 is moved, then the slots rotate by one.
 #pragma unroll 1

@@ -296,3 +296,36 @@ def test_hd_render_colour_matches_oracle(db, comp):
     res = _render_parity(db, comp, syn.hd_flame(0), 160, 90, (64.0,), channels=(0, 1, 2, 3))
     for (spp, c), (d, floor) in res.items():
         assert d < 1.25 * floor, (c, d, floor)
+
+
+@pytest.mark.parametrize("sort,flush", [(2, 0), (2, 1), (2, 2), (1, 2), (-1, 1)])
+def test_sort_and_flush_variants_agree(db, comp, sort, flush):
+    """Every (sort, flush) variant the autotuner may pick renders the same
+    flame: exact draw counts under a pass cap, the same density up to
+    Monte-Carlo noise (L1 within 1.25x the noise floor of two oracle seeds
+    against the default variant), and deterministic repeats."""
+    g = syn.hd_flame(1)
+    w, h = 160, 120
+    f = lr.flame.from_json(db, g)
+    base = comp.get_flame_kernel(db, f)
+    k = comp.get_flame_kernel(db, f, sort=sort, flush=flush)
+    chains_b = base.info["grid"] * base.info["block"] * base.info["chains_per_thread"]
+    chains_k = k.info["grid"] * k.info["block"] * k.info["chains_per_thread"]
+    passes = 64
+    dens = []
+    for kern, chains in ((base, chains_b), (k, chains_k), (k, chains_k)):
+        st = kern.warmup(f.pack_samples(4, w, h), (w, h), seed=11, count=20)
+        r = kern.bin(st, lr.bailout_args(iters=passes, millis=0, quality=0))
+        assert r.total_passes == passes * chains
+        b = st.bins().cpu().numpy().astype(np.float64)
+        assert abs(b[..., 3].sum() - r.draw_count) <= 1e-4 * r.draw_count
+        dens.append(b[..., 3])
+    np.testing.assert_array_equal(dens[1], dens[2])  # same variant twice: identical counts
+    a = dens[0] / dens[0].sum()
+    c = dens[1] / dens[1].sum()
+    # noise floor at this sample count from the oracle
+    p_ref, pal = orc.prepared(g, w, h)
+    o1, _ = orc.render(g, w, h, chains_k, passes, seed=1, threads=8, params=p_ref, palette=pal, hammersley=True)
+    o2, _ = orc.render(g, w, h, chains_k, passes, seed=2, threads=8, params=p_ref, palette=pal, hammersley=True)
+    floor = np.abs(o1[..., 3] / o1[..., 3].sum() - o2[..., 3] / o2[..., 3].sum()).sum()
+    assert np.abs(a - c).sum() < 1.25 * floor + 0.002, (np.abs(a - c).sum(), floor)
