@@ -42,6 +42,10 @@ METRIC = "iterations/s"
 WORKLOAD = "plain 1080p single flame: 1920x1080, 1024 spp, 8 xforms + final xform, 14-variation set, DE blur, tonemap"
 
 
+# dram__bytes_read.sum + dram__bytes_write.sum of one 1024-spp rfk_bin launch of
+# this workload (ncu, one pass; profiles/rfk_bin_1080p_launch_list.md)
+BIN_DRAM_BYTES_PER_LAUNCH = 39.30e6 + 40.45e3
+
 def _dist():
     ws = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -220,10 +224,11 @@ def run_gpu(args) -> dict:
         "e2e": {"value": e2e_passes / e2e_t, "unit": "iterations/s", "s_per_frame": e2e_t / args.steps,
                 "h2d_bytes_per_step": int(samples.nbytes), "d2h_bytes_per_step": int(W * H * 4 * 2)},
         "roofline": {"bound": "l2_atomic", "achieved": achieved_ops * 16 / 1e9, "peak": peak_ops * 16 / 1e9,
-                     "unit": "GB/s", "frac": achieved_ops / peak_ops, "traffic": None,
+                     "unit": "GB/s", "frac": achieved_ops / peak_ops, "traffic": BIN_DRAM_BYTES_PER_LAUNCH,
                      "achieved_ops": achieved_ops, "peak_ops": peak_ops,
                      "note": "red.global.add.v4.f32 payload (16 B per draw); peak = measured random red.v4 rate into a "
-                             "buffer of the histogram's size"},
+                             "buffer of the histogram's size; traffic = DRAM bytes of one 1024-spp rfk_bin "
+                             "launch from an ncu capture (the histogram stays in L2)"},
         "gpu_launches": args.steps * 3,
         "clocks": clocks.summary(),
         "draws_per_s": draws / t_total,
@@ -265,6 +270,142 @@ def cpu_baseline(genome: dict, seconds: float = 12.0, threads: int | None = None
             "draws_per_s": draws / dt, "seconds": dt, "iterations": iters}
 
 
+ANIM_WORKLOAD = ("batched animation: 120 frames 1280x720, 256 spp, Catmull-Rom over 4 keyframes (6 xforms, "
+                 "shared variation sets), one persistent launch, DE blur + tonemap, one CUDA graph")
+HETERO_WORKLOAD = ("heterogeneous batch: 64 flames, sizes 256^2..2048x1152, 2-12 xforms, 64/256/1024 spp, "
+                   "union-of-variations kernel, one persistent launch, DE blur + tonemap, one CUDA graph")
+
+
+def batch_workload(lr, db, name: str):
+    """(kernel genome, packed samples, units, workload text, tune genome + size)."""
+    units, samples = [], []
+    if name == "anim":
+        wl = load_workload("anim_720p.json")
+        w, h, n, spp = wl["width"], wl["height"], wl["frames"], float(wl["spp"])
+        keys = lr.align_flames(db, [lr.flame.from_json(db, g) for g in wl["keyframes"]])
+        ks = [f.pack_sample(w, h) for f in keys]
+        samples = np.stack([ks[0], ks[0], ks[1], ks[2], ks[3], ks[3]])
+        tp = keys[0].tonemap_params()
+        for i in range(n):
+            x = 3.0 * i / (n - 1)
+            seg = min(int(x), 2)
+            units.append(lr.batch_unit(w, h, spp, segment=seg, t=float(x - seg), gamma=tp["gamma"],
+                                       brightness=tp["brightness"], vibrancy=tp["vibrancy"]))
+        return keys[0], samples, units, ANIM_WORKLOAD, (keys[0], np.stack([ks[0]] * 4), (w, h))
+    wl = load_workload("hetero_64.json")
+    fl = wl["flames"]
+    al = lr.align_flames(db, [lr.flame.from_json(db, e["genome"]) for e in fl])
+    for i, (f, e) in enumerate(zip(al, fl)):
+        tp = f.tonemap_params()
+        units.append(lr.batch_unit(e["width"], e["height"], float(e["spp"]), segment=4 * i, t=0.0, gamma=tp["gamma"],
+                                   brightness=tp["brightness"], vibrancy=tp["vibrancy"]))
+        samples.append(f.pack_samples(4, e["width"], e["height"]).reshape(4, -1))
+    big = max(range(len(fl)), key=lambda i: fl[i]["width"] * fl[i]["height"] * fl[i]["spp"])
+    tune = (al[big], samples[big], (fl[big]["width"], fl[big]["height"]))
+    return al[0], np.concatenate(samples), units, HETERO_WORKLOAD, tune
+
+
+def run_batch(args) -> dict:
+    """Batched workloads (animation frames / heterogeneous flames): one batch
+    run = prepare + one persistent iterate launch + blur + tonemap per unit,
+    replayed as a CUDA graph; `value` times the graph on the device, `e2e`
+    adds the host sample copy and the read-back of every tonemapped image."""
+    import torch
+
+    from refraktor_gb300 import build
+    from refraktor_gb300 import librefrakt as lr
+
+    torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+    build.build()
+    db = lr.flamedb()
+    kf, samples, units, text, (tf, tsamples, tdims) = batch_workload(lr, db, args.workload)
+    tuned, tune_report = lr.autotune(db, tf, tsamples, tdims)
+    k = lr.flame_compiler().get_flame_kernel(db, kf, **tuned)
+    stream = torch.cuda.Stream()
+    flush = torch.empty(512 << 20 >> 2, dtype=torch.float32, device="cuda")
+    nsamples = samples.shape[0]
+    de = (9.0, 0.0, 0.5)
+
+    # schedule: queue-item length, one timed graph run each
+    sched = {}
+    for ppi in (128, 256, 512):
+        b = lr.batch(k, units, nsamples, passes_per_item=ppi, warmup=WARMUP_PASSES, de=de, out_format=lr.HALF4)
+        b.set_samples(samples)
+        b.run(use_graph=True, stream=stream)
+        b.wait()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        b.run(use_graph=True, stream=stream)
+        e1.record(stream)
+        tot, _ = b.wait()
+        sched[ppi] = tot.total_passes / (e0.elapsed_time(e1) / 1e3)
+        del b
+    ppi = max(sched, key=sched.get)
+    b = lr.batch(k, units, nsamples, passes_per_item=ppi, warmup=WARMUP_PASSES, de=de, out_format=lr.HALF4)
+    b.set_samples(samples)
+    info = b.info()
+
+    for _ in range(args.warmup):
+        b.run(use_graph=True, stream=stream)
+        b.wait()
+    times, passes, draws, kern_ms, reached = [], 0, 0, 0.0, True
+    with ClockSampler(int(os.environ.get("LOCAL_RANK", "0"))) as clocks:
+        for _ in range(args.steps):
+            _flush_l2(flush)
+            torch.cuda.synchronize()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            b.run(use_graph=True, stream=stream)
+            e1.record(stream)
+            tot, per = b.wait()
+            times.append(e0.elapsed_time(e1) / 1e3)
+            passes += tot.total_passes
+            draws += tot.draw_count
+            kern_ms += tot.elapsed_ms
+            reached = reached and bool(tot.status & 1)
+    t_total = sum(times)
+    info = b.info()
+
+    # e2e: host samples in, every tonemapped image out (pinned)
+    img_host = torch.empty(info["image_bytes"], dtype=torch.uint8, pin_memory=True)
+    img_dev = lr._device_view(lr.lib().rfk_batch_image(b._h, 0), (info["image_bytes"],), "|u1")
+    e2e_times, e2e_passes = [], 0
+    for i in range(args.warmup + args.steps):
+        _flush_l2(flush)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        b.set_samples(samples)
+        b.run(use_graph=True, stream=stream)
+        with torch.cuda.stream(stream):
+            img_host.copy_(img_dev, non_blocking=True)
+        tot, _ = b.wait()
+        stream.synchronize()
+        if i >= args.warmup:
+            e2e_times.append(time.perf_counter() - t0)
+            e2e_passes += tot.total_passes
+    e2e_t = sum(e2e_times)
+    peak_ops = lr.probe_red_v4(8 << 20, 512)
+    achieved_ops = draws / max(kern_ms / 1e3, 1e-9)
+    return {
+        "metric": METRIC, "value": passes / t_total, "unit": "iterations/s", "n_gpus": 1, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": 1e3 * t_total / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded genomes refraktor_gb300/workloads/)",
+        "config": {"workload": text, "units": len(units), "pixels": int(sum(u.width * u.height for u in units)),
+                   "grid": k.info["grid"], "block": k.info["block"], "chains_per_thread": k.info["chains_per_thread"],
+                   "flush": k.info["flush"], "sort": k.info["sort"], "autotune": tune_report,
+                   "passes_per_item": ppi, "schedule_iters_per_s": sched, "queue_items": info["items"],
+                   "l2": "512 MiB buffer written between timed steps", "all_units_reached_target": reached},
+        "e2e": {"value": e2e_passes / e2e_t, "unit": "iterations/s", "s_per_run": e2e_t / args.steps,
+                "s_per_unit": e2e_t / args.steps / len(units), "h2d_bytes_per_step": int(samples.nbytes),
+                "d2h_bytes_per_step": int(info["image_bytes"])},
+        "roofline": {"bound": "l2_atomic", "achieved": achieved_ops * 16 / 1e9, "peak": peak_ops * 16 / 1e9, "unit": "GB/s",
+                     "frac": achieved_ops / peak_ops, "traffic": None, "achieved_ops": achieved_ops, "peak_ops": peak_ops},
+        "gpu_launches": info["launches_per_run"] * args.steps,
+        "clocks": clocks.summary(),
+        "draws_per_s": draws / t_total,
+    }
+
+
 def run_reference(args) -> dict:
     """CPU reference leg: the FP64 oracle port on all host cores."""
     ws, rank = _dist()
@@ -293,8 +434,9 @@ def run_reference(args) -> dict:
 
 def run_ncu_case(args) -> None:
     """Small case for ncu captures of rfk_bin: the 1080p workload genome,
-    warm-up, then `--ncu-launches` bin launches to 16 spp each (~1 ms), with
-    the autotuned options unless --flush/--cpt/--block are given."""
+    warm-up, then `--ncu-launches` bin launches to `--ncu-spp` spp each
+    (16 spp: ~0.5 ms; 1024 spp is the bench step), with
+    the autotuned options unless --flush/--cpt/--block/--sort are given."""
     from refraktor_gb300 import build
     from refraktor_gb300 import librefrakt as lr
 
@@ -305,11 +447,11 @@ def run_ncu_case(args) -> None:
     if args.flush is None:
         opts, _ = lr.autotune(db, f, samples, (W, H))
     else:
-        opts = dict(flush=args.flush, chains_per_thread=args.cpt, block=args.block)
+        opts = dict(flush=args.flush, chains_per_thread=args.cpt, block=args.block, sort=args.sort)
     k = lr.flame_compiler().get_flame_kernel(db, f, **opts)
     st = k.warmup(samples, (W, H), 1, WARMUP_PASSES)
     for _ in range(args.ncu_launches):
-        r = k.bin(st, lr.bailout_args(iters=0, millis=0, quality=16.0))
+        r = k.bin(st, lr.bailout_args(iters=0, millis=0, quality=float(args.ncu_spp)))
     print(json.dumps({"ncu_case": k.info, "opts": opts, "passes": r.total_passes, "ms": r.elapsed_ms}))
 
 
@@ -317,20 +459,29 @@ def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--ncu-case", action="store_true")
     ap.add_argument("--ncu-launches", type=int, default=2)
+    ap.add_argument("--ncu-spp", type=int, default=16)
     ap.add_argument("--flush", type=int, default=None)
     ap.add_argument("--cpt", type=int, default=4)
     ap.add_argument("--block", type=int, default=256)
+    ap.add_argument("--sort", type=int, default=2)
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--workload", default="hd", choices=["hd", "anim", "hetero"],
+                    help="hd: the 1080p single-flame bench (default); anim / hetero: the batched workloads")
     args = ap.parse_args()
     if args.ncu_case:
         run_ncu_case(args)
         return
-    line = run_reference(args) if args.impl == "reference" else run_gpu(args)
+    if args.impl == "reference":
+        line = run_reference(args)
+    elif args.workload != "hd":
+        line = run_batch(args)
+    else:
+        line = run_gpu(args)
     if line:
         print(json.dumps(line))
 

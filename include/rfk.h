@@ -86,8 +86,10 @@ typedef struct {
     int block;             /* threads per block (0 = 256) */
     int chains_per_thread; /* 0 = 4 when sorting, else 1 */
     int flush;             /* histogram update: 0 = red.global.add.v4.f32 per draw, 1 = warp-aggregated,
-                              2 = warp-aggregated into a per-block shared-memory cache of hot pixels */
-    int blocks_per_sm;     /* 0 = as many as fit */
+                              2 = warp-aggregated into a per-block shared-memory cache of hot pixels,
+                              3 = the shared-memory cache without warp aggregation */
+    int blocks_per_sm;     /* 0 = as many as fit; n > 0 = at most n bin blocks per SM, and
+                              registers capped so that n fit (launch bounds) */
     int sort;              /* 0 or 1 = sort each warp's chains by xform every pass, 2 = sort the whole
                               block's chains (both when 2..32 xforms); -1 = never */
 } rfk_compile_opts;
@@ -116,7 +118,8 @@ rfk_status rfk_kernel_get_info(const rfk_kernel* k, rfk_kernel_info* out);
  * bodies); needs no device. */
 rfk_status rfk_generate_source(const rfk_db* db, const rfk_flame* f, char* buf, size_t cap, size_t* len);
 /* NVRTC-compiles the flame's kernels for `arch` (e.g. "sm_103a") without
- * loading them: a compile check that needs no device. */
+ * loading them: a compile check that needs no device. The log holds the
+ * compiler's per-kernel resource report (registers, spills, shared memory). */
 rfk_status rfk_compile_check(const rfk_db* db, const rfk_flame* f, const rfk_compile_opts* opts, const char* arch, char* log,
                              size_t log_cap);
 /* The generated device source (flame_compiler::result::source). */
@@ -268,6 +271,87 @@ typedef struct {
 } rfk_tune_report;
 rfk_status rfk_autotune(const rfk_db* db, const rfk_flame* f, const double* samples, size_t nsamples, uint32_t w, uint32_t h,
                         uint32_t passes, rfk_compile_opts* best, rfk_tune_report* report);
+
+/* ---- structure alignment ---------------------------------------------------
+ * Gives n genomes one structure (xform count, vlink chains, variation sets,
+ * final xform, chaos rows) without changing what each renders, so they pack
+ * to one layout: keyframes of different structure can be interpolated, and
+ * unrelated flames share one (union-of-variations) kernel in a batch.
+ * Replaces the interpolator's rebuild_sides / interp_xforms
+ * (src/refraktor/src/refraktor.cpp:117-191) with flamedb::make_padder
+ * (src/librefrakt/src/flame_info.cpp:239-320), generalised from two genomes
+ * to n. by_weight != 0: each genome gets all genomes' xforms, the foreign ones
+ * with weight 0; otherwise xforms align by position and missing vlinks are
+ * padded. out receives n new handles (rfk_flame_destroy each). */
+rfk_status rfk_flames_align(const rfk_db* db, const rfk_flame* const* flames, size_t n, int by_weight, rfk_flame** out);
+
+/* ---- batched rendering -----------------------------------------------------
+ * No reference counterpart: the reference renders one flame per
+ * flame_kernel::bin call (flame_compiler.h:92-98). A batch renders many units
+ * (flames or animation frames) of the kernel's structure in one persistent
+ * launch: each unit's parameter block is the spline of the batch's packed
+ * samples at (segment, t), evaluated on the device; every unit iterates into
+ * its own histogram until its quality target, then gets its own
+ * density-estimation blur and tonemap. rfk_batch_run enqueues the whole
+ * pipeline (sample upload, rotation fix-up, spline, prepare, clear, iterate,
+ * blur, tonemap, counter read-back) on a stream, directly or as one CUDA
+ * graph captured on the first run and replayed afterwards. */
+typedef struct rfk_batch rfk_batch;
+
+typedef struct {
+    uint32_t width, height;  /* image size */
+    double quality;          /* target samples per pixel (as rfk_bailout.quality), > 0 */
+    uint32_t segment;        /* spline segment: samples segment .. segment + 3, interpolating
+                                between samples segment + 1 and segment + 2 */
+    float t;                 /* position in the segment, [0, 1] */
+    float gamma, brightness, vibrancy, highlight_power; /* tonemap parameters of this unit */
+} rfk_batch_unit;
+
+typedef struct {
+    uint32_t passes_per_item; /* passes of one block's chains per queue item; 0 = 256 */
+    uint32_t warmup;          /* passes without drawing for chains new to a unit */
+    uint32_t seed;
+    uint32_t millis;          /* time budget of the iterate launch; 0 or > 60000 = 60000 */
+    float de_max_radius;      /* density-estimation blur (as rfk_de_args); 0 = none */
+    float de_min_radius;
+    float de_curve;
+    int out_format;           /* RFK_HALF3 .. RFK_FLOAT4, or -1 = histograms only */
+    int precise_tonemap;      /* as rfk_tonemap_args.precise */
+    uint32_t item_factor;     /* queue items per unit as a multiple of the least needed at
+                                 full efficiency; 0 = 3 (units whose draws fall short of
+                                 1 / item_factor of the iterations may end below target) */
+} rfk_batch_opts;
+
+typedef struct {
+    size_t units;
+    uint64_t items;           /* queue length */
+    size_t hist_bytes;        /* device bytes of all histograms */
+    size_t image_bytes;       /* device bytes of all tonemapped images */
+    int launches_per_run;     /* kernel launches of one run (graph nodes that are kernels) */
+    int graph;                /* 1 once the pipeline is captured as a CUDA graph */
+} rfk_batch_info;
+
+/* nsamples packed samples (n x (size_reals + 768) doubles, the kernel's
+ * layout) are given per run by rfk_batch_set_samples. */
+rfk_status rfk_batch_create(rfk_kernel* k, const rfk_batch_unit* units, size_t nunits, size_t nsamples,
+                            const rfk_batch_opts* opts, rfk_batch** out);
+void rfk_batch_destroy(rfk_batch* b);
+/* Copies the samples (nsamples x (size_reals + 768) doubles, as given to
+ * rfk_batch_create) into the batch's pinned staging; the next run uploads them. */
+rfk_status rfk_batch_set_samples(rfk_batch* b, const double* samples);
+/* Enqueues one run on `stream` (cudaStream_t). use_graph != 0 captures the
+ * pipeline as a CUDA graph on the first such run and replays it later. */
+rfk_status rfk_batch_run(rfk_batch* b, int use_graph, void* stream);
+/* Waits for the last run; fills the totals and, when per_unit is non-null,
+ * one result per unit (quality = accumulated spp of the unit; status has
+ * RFK_ST_QUALITY-like bit 1 set when the unit reached its target). */
+rfk_status rfk_batch_wait(rfk_batch* b, rfk_bin_result* total, rfk_bin_result* per_unit);
+/* Device pointers of unit u: histogram (float4 w x h), tonemapped image (NULL
+ * when out_format < 0), prepared parameter block (floats, without jitter). */
+void* rfk_batch_bins(rfk_batch* b, size_t unit);
+void* rfk_batch_image(rfk_batch* b, size_t unit);
+void* rfk_batch_params(rfk_batch* b, size_t unit);
+rfk_status rfk_batch_get_info(const rfk_batch* b, rfk_batch_info* info);
 
 /* ---- measurement helpers -------------------------------------------------- */
 /* red.global.add.v4.f32 operations per second into a device buffer of

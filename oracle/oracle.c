@@ -236,7 +236,10 @@ static double apply_xf(const flame_desc* d, const double* P, int xi, double* x, 
         const double px = A[0] * ix + A[2] * iy + A[4];
         const double py = A[1] * ix + A[3] * iy + A[5];
         double rx = 0.0, ry = 0.0;
-        for (int v = 0; v < xf->n_vars[l]; v++) variation(xf->var_id[l][v], P, xf->var_off[l][v], px, py, &rx, &ry, u, used);
+        /* a zero-weight variation adds nothing and draws no uniforms (the
+           generated kernels skip it the same way) */
+        for (int v = 0; v < xf->n_vars[l]; v++)
+            if (P[xf->var_off[l][v]] != 0.0) variation(xf->var_id[l][v], P, xf->var_off[l][v], px, py, &rx, &ry, u, used);
         ix = rx;
         iy = ry;
     }

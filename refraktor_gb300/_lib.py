@@ -51,6 +51,23 @@ class DEArgs(C.Structure):
     _fields_ = [("max_radius", C.c_double), ("min_radius", C.c_double), ("curve", C.c_double)]
 
 
+class BatchUnit(C.Structure):
+    _fields_ = [("width", C.c_uint32), ("height", C.c_uint32), ("quality", C.c_double), ("segment", C.c_uint32),
+                ("t", C.c_float), ("gamma", C.c_float), ("brightness", C.c_float), ("vibrancy", C.c_float),
+                ("highlight_power", C.c_float)]
+
+
+class BatchOpts(C.Structure):
+    _fields_ = [("passes_per_item", C.c_uint32), ("warmup", C.c_uint32), ("seed", C.c_uint32), ("millis", C.c_uint32),
+                ("de_max_radius", C.c_float), ("de_min_radius", C.c_float), ("de_curve", C.c_float),
+                ("out_format", C.c_int), ("precise_tonemap", C.c_int), ("item_factor", C.c_uint32)]
+
+
+class BatchInfo(C.Structure):
+    _fields_ = [("units", C.c_size_t), ("items", C.c_uint64), ("hist_bytes", C.c_size_t), ("image_bytes", C.c_size_t),
+                ("launches_per_run", C.c_int), ("graph", C.c_int)]
+
+
 # name -> (restype, argtypes)
 SIGNATURES = {
     "rfk_last_error": (C.c_char_p, []),
@@ -102,6 +119,17 @@ SIGNATURES = {
     "rfk_device_sm_count": (C.c_int, []),
     "rfk_autotune": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_size_t, C.c_uint32, C.c_uint32, C.c_uint32,
                                C.POINTER(CompileOpts), C.POINTER(TuneReport)]),
+    "rfk_flames_align": (C.c_int, [C.c_void_p, C.POINTER(C.c_void_p), C.c_size_t, C.c_int, C.POINTER(C.c_void_p)]),
+    "rfk_batch_create": (C.c_int, [C.c_void_p, C.POINTER(BatchUnit), C.c_size_t, C.c_size_t, C.POINTER(BatchOpts),
+                                   C.POINTER(C.c_void_p)]),
+    "rfk_batch_destroy": (None, [C.c_void_p]),
+    "rfk_batch_set_samples": (C.c_int, [C.c_void_p, C.c_void_p]),
+    "rfk_batch_run": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p]),
+    "rfk_batch_wait": (C.c_int, [C.c_void_p, C.POINTER(BinResult), C.POINTER(BinResult)]),
+    "rfk_batch_bins": (C.c_void_p, [C.c_void_p, C.c_size_t]),
+    "rfk_batch_image": (C.c_void_p, [C.c_void_p, C.c_size_t]),
+    "rfk_batch_params": (C.c_void_p, [C.c_void_p, C.c_size_t]),
+    "rfk_batch_get_info": (C.c_int, [C.c_void_p, C.POINTER(BatchInfo)]),
 }
 
 

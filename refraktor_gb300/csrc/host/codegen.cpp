@@ -73,7 +73,12 @@ struct emitter {
                     fn << "            const R P_" << plain[i] << " = P[" << v0 + 1 + i << "]; (void)P_" << plain[i] << ";\n";
                 for (size_t i = 0; i < pre.size(); i++)
                     fn << "            const R P_" << pre[i] << " = P[" << v0 + 1 + plain.size() + i << "]; (void)P_" << pre[i] << ";\n";
-                fn << indent(dsl::emit_body(*def.apply_ast, env), 3);
+                // a zero-weight variation (padding, or a union kernel's slot
+                // that this flame does not use) adds nothing and draws no
+                // random numbers; skipping it also keeps 0 * inf out of the sum
+                fn << "            if (w_ != R(0)) {\n";
+                fn << indent(dsl::emit_body(*def.apply_ast, env), 4);
+                fn << "            }\n";
                 fn << "        }\n";
                 info.rand_calls += def.apply_usage.rand_calls;
                 info.sfu_ops += def.apply_usage.sfu_ops;

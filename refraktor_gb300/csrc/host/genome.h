@@ -98,6 +98,17 @@ flame flame_from_flam3(const flamedb& db, const std::string& xml);
 // New vardata with defaults for `name` (flame_info.cpp:224-237).
 vardata make_vardata(const flamedb& db, const std::string& name);
 
+// A vlink that maps (nearly) as the identity but carries the variations of
+// `vl`, to pad a vlink chain (flamedb::make_padder, flame_info.cpp:239-320).
+vlink make_padder(const flamedb& db, const vlink& vl);
+
+// Gives genomes one structure (xform count, vlink chains, variation sets,
+// final xform, chaos rows) without changing what each one renders: the
+// reference interpolator's alignment (src/refraktor/src/refraktor.cpp:117-191)
+// for any number of genomes. by_weight: every genome carries all genomes'
+// xforms, the foreign ones with weight 0; otherwise xforms align by position.
+std::vector<flame> align_structures(const flamedb& db, const std::vector<flame>& flames, bool by_weight);
+
 // FP64 rotation fix-up of packed samples before spline interpolation
 // (src/librefrakt/src/flame_compiler.cpp:957-1035): every affine's linear
 // columns become (angle, log magnitude) with angles unwrapped across samples,

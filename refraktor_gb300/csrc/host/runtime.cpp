@@ -24,67 +24,20 @@
 #include "codegen.h"
 #include "flamedb.h"
 #include "genome.h"
+#include "runtime_internal.h"
 
 extern const char* const rfk_src_device;
 extern const char* const rfk_src_iterate;
 
 namespace {
-
 thread_local std::string g_error;
+}  // namespace
 
-struct rfk_exception : std::runtime_error {
-    rfk_status code;
-    rfk_exception(rfk_status c, const std::string& m) : std::runtime_error(m), code(c) {}
-};
+std::string& rfk::rt::error_message() { return g_error; }
 
-[[noreturn]] void fail(rfk_status c, const std::string& m) { throw rfk_exception(c, m); }
+using namespace rfk::rt;
 
-void cuda_check(cudaError_t e, const char* what) {
-    if (e != cudaSuccess) fail(RFK_E_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
-}
-
-
-template <typename F>
-rfk_status guard(F&& f) {
-    try {
-        g_error.clear();
-        f();
-        return RFK_OK;
-    } catch (const rfk_exception& e) {
-        g_error = e.what();
-        return e.code;
-    } catch (const rfk::format_error& e) {
-        g_error = e.what();
-        return RFK_E_FORMAT;
-    } catch (const rfk::dsl::parse_error& e) {
-        g_error = e.what();
-        return RFK_E_FORMAT;
-    } catch (const std::bad_alloc&) {
-        g_error = "out of host memory";
-        return RFK_E_INVALID;
-    } catch (const std::exception& e) {
-        g_error = e.what();
-        return RFK_E_INVALID;
-    }
-}
-
-int device_sm_count() {
-    int dev = 0, n = 0;
-    cuda_check(cudaGetDevice(&dev), "cudaGetDevice");
-    cuda_check(cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev), "cudaDeviceGetAttribute");
-    return n;
-}
-
-std::string device_arch() {
-    int dev = 0, major = 0, minor = 0;
-    cudaError_t e = cudaGetDevice(&dev);
-    if (e != cudaSuccess) fail(RFK_E_NODEVICE, std::string("no CUDA device: ") + cudaGetErrorString(e));
-    cuda_check(cudaDeviceGetAttribute(&major, cudaDevAttrComputeCapabilityMajor, dev), "compute capability");
-    cuda_check(cudaDeviceGetAttribute(&minor, cudaDevAttrComputeCapabilityMinor, dev), "compute capability");
-    if (major < 10) fail(RFK_E_NODEVICE, "device compute capability " + std::to_string(major) + "." + std::to_string(minor) +
-                                             " is below the sm_100 family this library targets");
-    return "sm_" + std::to_string(major) + std::to_string(minor) + "a";
-}
+namespace {
 
 // Host mirror of rfk_chains / rfk_bin_args / rfk_counters in rfk_iterate.cuh.
 struct dev_chains {
@@ -112,35 +65,6 @@ constexpr uint32_t kMaxBinMillis = 60000;  // upper bound of one bin call
 
 }  // namespace
 
-// ------------------------------------------------------------------ handles --
-struct rfk_db {
-    rfk::flamedb db;
-};
-
-struct rfk_flame {
-    rfk::flame f;
-};
-
-struct kernel_impl {
-    rfk::generated_flame gen;
-    std::string source;
-    std::string log;
-    cudaLibrary_t lib = nullptr;
-    cudaKernel_t f_prepare = nullptr, f_warmup = nullptr, f_bin = nullptr, f_apply = nullptr;
-    int block = 256, cpt = 1, flush = 0, sort = 0, grid = 0, regs = 0;
-    size_t sample_floats = 0;
-    double compile_ms = 0.0;
-    double sfu_per_iter = 0.0;
-    uint32_t salt = 0;
-    ~kernel_impl() {
-        if (lib) cudaLibraryUnload(lib);
-    }
-};
-
-struct rfk_kernel {
-    std::shared_ptr<kernel_impl> impl;
-};
-
 struct rfk_state {
     std::shared_ptr<const kernel_impl> k;
     unsigned w = 0, h = 0, seed = 0;
@@ -157,7 +81,6 @@ struct rfk_state {
     cudaEvent_t done = nullptr;
     unsigned call_id = 0;
     double quality = 0.0;
-    unsigned long long warmup_hits = 0;
     bool pending = false;
 
     ~rfk_state() {
@@ -186,14 +109,19 @@ std::string full_source(const rfk::generated_flame& g) {
 }
 
 std::vector<char> nvrtc_build(const std::string& source, const std::string& arch_name, const rfk_compile_opts& o, int block,
-                              int cpt, int flush, int sort, std::string& log) {
+                              int cpt, int flush, int sort, std::string& log, bool verbose = false) {
     const std::string arch = "--gpu-architecture=" + arch_name;
     const std::string d_block = "-DRFK_BLOCK=" + std::to_string(block);
     const std::string d_cpt = "-DRFK_CPT=" + std::to_string(cpt);
     const std::string d_flush = "-DRFK_FLUSH=" + std::to_string(flush);
     const std::string d_sort = "-DRFK_SORT=" + std::to_string(sort);
+    // blocks_per_sm > 0 also asks the compiler to fit that many bin blocks per
+    // SM (registers capped through the launch bounds)
+    const std::string d_minb = "-DRFK_MINB=" + std::to_string(o.blocks_per_sm);
     std::vector<const char*> opts = {arch.c_str(), "-std=c++17", "-lineinfo", d_block.c_str(), d_cpt.c_str(),
                                      d_flush.c_str(), d_sort.c_str(), "-extra-device-vectorization"};
+    if (o.blocks_per_sm > 0) opts.push_back(d_minb.c_str());
+    if (verbose) opts.push_back("--ptxas-options=-v");  // per-kernel registers / spills / shared memory in the log
     if (!o.precise_math) {
         opts.push_back("--use_fast_math");
         opts.push_back("-DRFK_FAST_HYPOT=1");
@@ -237,8 +165,9 @@ void check_options(const rfk_compile_opts& o) {
     const int block = o.block > 0 ? o.block : 256;
     if (block % 32 != 0 || block > 1024) fail(RFK_E_INVALID, "block must be a multiple of 32 up to 1024");
     if (o.chains_per_thread > 8 || o.chains_per_thread < 0) fail(RFK_E_INVALID, "chains_per_thread must be in [0, 8]");
-    if (o.flush < 0 || o.flush > 2) fail(RFK_E_INVALID, "flush must be 0, 1 or 2");
-    if (o.blocks_per_sm < 0) fail(RFK_E_INVALID, "negative option");
+    if (o.flush < 0 || o.flush > 3) fail(RFK_E_INVALID, "flush must be 0, 1, 2 or 3");
+    if (o.blocks_per_sm < 0 || o.blocks_per_sm > 32) fail(RFK_E_INVALID, "blocks_per_sm must be in [0, 32]");
+    if (o.blocks_per_sm * block > 2048) fail(RFK_E_INVALID, "blocks_per_sm x block exceeds 2048 threads per SM");
 }
 
 // NVRTC module cache: (db hash, structure, options) -> kernel.
@@ -267,6 +196,7 @@ std::shared_ptr<kernel_impl> compile(const rfk::flamedb& db, const rfk::flame& f
     cuda_check(cudaLibraryGetKernel(&k->f_warmup, k->lib, "rfk_warmup"), "rfk_warmup");
     cuda_check(cudaLibraryGetKernel(&k->f_bin, k->lib, "rfk_bin"), "rfk_bin");
     cuda_check(cudaLibraryGetKernel(&k->f_apply, k->lib, "rfk_apply"), "rfk_apply");
+    cuda_check(cudaLibraryGetKernel(&k->f_bin_batch, k->lib, "rfk_bin_batch"), "rfk_bin_batch");
     cudaFuncAttributes fa{};
     cuda_check(cudaFuncGetAttributes(&fa, reinterpret_cast<const void*>(k->f_bin)), "attributes");
     k->regs = fa.numRegs;
@@ -304,10 +234,6 @@ std::shared_ptr<kernel_impl> compile_cached(const rfk::flamedb& db, const rfk::f
     std::lock_guard<std::mutex> lk(g_cache_mu);
     g_cache[key.str()] = k;
     return k;
-}
-
-void launch(cudaKernel_t fn, unsigned grid, unsigned block, cudaStream_t s, void** args, const char* what) {
-    cuda_check(cudaLaunchKernel(reinterpret_cast<const void*>(fn), dim3(grid), dim3(block), args, 0, s), what);
 }
 
 // Temporal sample s of S: spline segment and t within it, as refactor.cu:266-270.
@@ -352,8 +278,8 @@ void prepare(const kernel_impl& k, const double* samples, size_t nsamples, const
     cuda_check(cudaMemcpyAsync(d_seg, seg.data(), seg.size() * sizeof(unsigned), cudaMemcpyHostToDevice, s), "H2D schedule");
     cuda_check(cudaMemcpyAsync(d_t, t.data(), t.size() * sizeof(float), cudaMemcpyHostToDevice, s), "H2D schedule");
     cuda_check(rfk_launch_catmull(d_samples, (unsigned)sample_size, nseg, d_coeff, s), "catmull");
-    unsigned ss = (unsigned)sample_size, salt = k.salt;
-    void* args[] = {&d_coeff, &ss, &d_seg, &d_t, &d_out, &seed, &salt};
+    unsigned ss = (unsigned)sample_size, salt = k.salt, jitter = 1;
+    void* args[] = {&d_coeff, &ss, &d_seg, &d_t, &d_out, &seed, &salt, &jitter};
     launch(k.f_prepare, (unsigned)seg.size(), 256, s, args, "rfk_prepare");
     // the host vectors must outlive the copies
     cuda_check(cudaStreamSynchronize(s), "prepare");
@@ -535,7 +461,7 @@ rfk_status rfk_compile_check(const rfk_db* db, const rfk_flame* f, const rfk_com
         check_options(o);
         auto g = rfk::generate_flame_code(db->db, f->f);
         const int sort = resolve_sort(o, g.num_xforms);
-        nvrtc_build(full_source(g), arch, o, o.block > 0 ? o.block : 256, resolve_cpt(o, sort), o.flush, sort, nlog);
+        nvrtc_build(full_source(g), arch, o, o.block > 0 ? o.block : 256, resolve_cpt(o, sort), o.flush, sort, nlog, true);
     });
     if (log && log_cap) copy_out(log, log_cap, nullptr, st == RFK_OK ? nlog : g_error);
     return st;
@@ -602,10 +528,8 @@ rfk_status rfk_warmup(const rfk_kernel* kh, const double* samples, size_t nsampl
         cuda_check(cudaEventCreateWithFlags(&st->done, cudaEventDisableTiming), "event");
         dev_chains ch{st->d_x, st->d_y, st->d_c, st->d_last};
         unsigned ww = w, hh = h, sd = seed, salt = k->salt, wc = warmup_count;
-        unsigned long long* wh = st->d_counters + kCounterWords + 97;
-        void* args[] = {&st->d_samples, &ch, &ww, &hh, &sd, &salt, &wc, &wh};
+        void* args[] = {&st->d_samples, &ch, &ww, &hh, &sd, &salt, &wc};
         launch(k->f_warmup, (unsigned)st->grid, (unsigned)k->block, s, args, "rfk_warmup");
-        cuda_check(cudaMemcpyAsync(&st->warmup_hits, wh, sizeof(unsigned long long), cudaMemcpyDeviceToHost, s), "D2H");
         cuda_check(cudaStreamSynchronize(s), "warmup");
         *out = st.release();
     });
@@ -815,8 +739,8 @@ rfk_status rfk_prepare_samples_noalloc(const rfk_kernel* kh, const double* sampl
                                            (unsigned)naff, s),
                    "fix_rotation");
         cuda_check(rfk_launch_catmull(d_samples, (unsigned)ss, (unsigned)nseg, d_coeff, s), "catmull");
-        unsigned sz = (unsigned)ss, salt = k.salt, sd = seed;
-        void* args[] = {&d_coeff, &sz, &d_seg, &d_t, &d_out, &sd, &salt};
+        unsigned sz = (unsigned)ss, salt = k.salt, sd = seed, jitter = 1;
+        void* args[] = {&d_coeff, &sz, &d_seg, &d_t, &d_out, &sd, &salt, &jitter};
         launch(k.f_prepare, (unsigned)count, 256, s, args, "rfk_prepare");
         cuda_check(cudaMemcpyAsync(out, d_out, count * k.sample_floats * sizeof(float), cudaMemcpyDeviceToHost, s), "D2H");
         cuda_check(cudaStreamSynchronize(s), "prepare");
@@ -835,7 +759,8 @@ rfk_status rfk_tonemap(const float* bins, uint32_t w, uint32_t h, void* out, int
         const float scale_constant = std::pow(10.0f, -std::log10((float)a->quality) - 0.5f);
         cuda_check(rfk_launch_tonemap(reinterpret_cast<const float4*>(bins), w * h, out, format, a->precise, (float)a->gamma,
                                       scale_constant, (float)a->brightness, (float)a->vibrancy, (float)a->highlight_power,
-                                      (unsigned long long*)histogram, (unsigned long long*)max_density, (cudaStream_t)stream),
+                                      (unsigned long long*)histogram, (unsigned long long*)max_density, nullptr, 0.0,
+                                      (cudaStream_t)stream),
                    "tonemap");
     });
 }
@@ -920,7 +845,7 @@ rfk_status rfk_autotune(const rfk_db* db, const rfk_flame* f, const double* samp
                         uint32_t passes, rfk_compile_opts* best, rfk_tune_report* report) {
     return guard([&] {
         if (!db || !f || !samples || !best) fail(RFK_E_INVALID, "null argument");
-        if (passes == 0) passes = 32;
+        if (passes == 0) passes = 256;
         const size_t ss = f->f.size_reals() + rfk::palette_reals;
         std::ostringstream key;
         key << db->db.hash() << "|" << f->f.structure_key() << "|" << w << "x" << h << "|" << passes << "|";
@@ -941,9 +866,9 @@ rfk_status rfk_autotune(const rfk_db* db, const rfk_flame* f, const double* samp
                 return;
             }
         }
-        struct cand { int block, cpt, flush, sort; };
-        const cand cands[] = {{256, 4, 0, 1}, {256, 4, 1, 1}, {256, 4, 2, 1}, {128, 4, 1, 1},
-                              {256, 4, 0, 2}, {256, 4, 1, 2}, {256, 4, 2, 2}, {512, 2, 1, 2}};
+        struct cand { int block, cpt, flush, sort, minb; };
+        const cand cands[] = {{256, 4, 0, 2, 0}, {256, 4, 1, 2, 0}, {256, 4, 2, 2, 0}, {256, 4, 3, 2, 0},
+                              {256, 4, 1, 1, 0}, {512, 2, 0, 2, 0}, {256, 4, 0, 2, 5}, {256, 4, 1, 2, 5}};
         double best_rate = -1.0, worst_rate = 1e300;
         int n = 0;
         for (const cand& c : cands) {
@@ -952,6 +877,7 @@ rfk_status rfk_autotune(const rfk_db* db, const rfk_flame* f, const double* samp
             o.chains_per_thread = c.cpt;
             o.flush = c.flush;
             o.sort = c.sort;
+            o.blocks_per_sm = c.minb;
             rfk_kernel* kh = nullptr;
             if (rfk_compile(db, f, &o, &kh, nullptr, 0) != RFK_OK) continue;
             rfk_state* st = nullptr;

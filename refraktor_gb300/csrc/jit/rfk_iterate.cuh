@@ -9,7 +9,9 @@
 //   void rfk_precalc(float* P, Rng& rng)                             (variation precalc)
 // and the launch shape: RFK_BLOCK (threads per block), RFK_CPT (chains per
 // thread), RFK_FLUSH (0 = one red.global.add.v4.f32 per draw, 1 = warp-
-// aggregated red for lanes that hit the same pixel), RFK_SORT (1 = sort each
+// aggregated red for lanes that hit the same pixel, 2 = warp-aggregated into a
+// per-block shared-memory cache of hot pixels, 3 = the cache without warp
+// aggregation), RFK_SORT (1 = sort each
 // warp's chains by picked xform every pass, so a warp runs one xform at a
 // time instead of a divergent switch).
 //
@@ -88,10 +90,12 @@ struct rfk_chains {
 
 // ---------------------------------------------------------------- prepare --
 // One block per temporal sample: evaluate the spline segment at t, convert
-// affines, build the palette, run precalc, build the xform pick tables.
+// affines, build the palette, run precalc, build the xform pick tables, and
+// (jitter != 0) offset the screen affine by the sample's antialiasing jitter.
 extern "C" __global__ void __launch_bounds__(256) rfk_prepare(const float4* __restrict__ coeff, unsigned sample_size,
                                                               const unsigned* __restrict__ seg_of, const float* __restrict__ t_of,
-                                                              float* __restrict__ out, unsigned seed, unsigned salt) {
+                                                              float* __restrict__ out, unsigned seed, unsigned salt,
+                                                              unsigned jitter) {
     __shared__ float P[RFK_SAMPLE_FLOATS];
     const unsigned s = blockIdx.x;
     const float t = t_of[s];
@@ -180,8 +184,10 @@ extern "C" __global__ void __launch_bounds__(256) rfk_prepare(const float4* __re
 #endif
         // screen jitter ~ gauss(1/3 px) for antialiasing (flame.tpl:179-182)
         V2 j = rng.gauss(1.0f / 3.0f);
-        P[4] += j.x;
-        P[5] += j.y;
+        if (jitter) {
+            P[4] += j.x;
+            P[5] += j.y;
+        }
         rfk_precalc(P, rng);
     }
     __syncthreads();
@@ -384,7 +390,7 @@ __device__ __forceinline__ void rfk_block_sort(float (&x)[RFK_CPT], float (&y)[R
 }
 #endif
 
-#if RFK_FLUSH == 2
+#if RFK_FLUSH >= 2
 // Shared-memory cache of hot pixels (one per block): direct-mapped slots keyed
 // by pixel index, claimed with atomicCAS while empty and never evicted until
 // the next flush, so adds into a claimed slot never race with its flush.
@@ -418,14 +424,35 @@ __device__ __forceinline__ void rfk_cache_flush(rfk_cache& cc, float4* __restric
         }
     }
 }
+
+// Adds one contribution through the block's hot-pixel cache: into the slot of
+// `idx` when it holds idx or can be claimed, else straight to the histogram.
+__device__ __forceinline__ void rfk_cache_add(rfk_cache& cc, float4* __restrict__ bins, int idx, float4 acc) {
+    const unsigned slot = rfk_cache_slot(idx);
+    unsigned t = cc.tag[slot];
+    if (t == RFK_CACHE_EMPTY) {
+        t = atomicCAS(&cc.tag[slot], RFK_CACHE_EMPTY, (unsigned)idx);
+        if (t == RFK_CACHE_EMPTY) t = (unsigned)idx;
+    }
+    if (t == (unsigned)idx) {
+        atomicAdd(&cc.val[0][slot], acc.x);
+        atomicAdd(&cc.val[1][slot], acc.y);
+        atomicAdd(&cc.val[2][slot], acc.z);
+        atomicAdd(&cc.val[3][slot], acc.w);
+    } else {
+        rfk_red_v4(bins + idx, acc.x, acc.y, acc.z, acc.w);
+    }
+}
 #endif
 
 __device__ __forceinline__ void rfk_flush(float4* __restrict__ bins, int idx, float4 v
-#if RFK_FLUSH == 2
+#if RFK_FLUSH >= 2
                                           , rfk_cache& cc
 #endif
 ) {
-#if RFK_FLUSH >= 1
+#if RFK_FLUSH == 3
+    if (idx >= 0) rfk_cache_add(cc, bins, idx, v);
+#elif RFK_FLUSH >= 1
     // lanes that hit the same pixel add their contributions first
     const unsigned active = __activemask();
     const unsigned same = __match_any_sync(active, idx);
@@ -446,20 +473,7 @@ __device__ __forceinline__ void rfk_flush(float4* __restrict__ bins, int idx, fl
         }
         if ((int)lane == leader) {
 #if RFK_FLUSH == 2
-            const unsigned slot = rfk_cache_slot(idx);
-            unsigned t = cc.tag[slot];
-            if (t == RFK_CACHE_EMPTY) {
-                t = atomicCAS(&cc.tag[slot], RFK_CACHE_EMPTY, (unsigned)idx);
-                if (t == RFK_CACHE_EMPTY) t = (unsigned)idx;
-            }
-            if (t == (unsigned)idx) {
-                atomicAdd(&cc.val[0][slot], acc.x);
-                atomicAdd(&cc.val[1][slot], acc.y);
-                atomicAdd(&cc.val[2][slot], acc.z);
-                atomicAdd(&cc.val[3][slot], acc.w);
-            } else {
-                rfk_red_v4(bins + idx, acc.x, acc.y, acc.z, acc.w);
-            }
+            rfk_cache_add(cc, bins, idx, acc);
 #else
             rfk_red_v4(bins + idx, acc.x, acc.y, acc.z, acc.w);
 #endif
@@ -478,54 +492,6 @@ __device__ __forceinline__ V2 rfk_hammersley(unsigned idx, unsigned total) {
     float inv = 1.0f / (float)max_val;
     unsigned flipped = (radix == 0u) ? 0u : (__brev(idx) >> (32u - radix));
     return fl_vec2((float)idx * inv * 2.0f - 1.0f, (float)flipped * inv * 2.0f - 1.0f);
-}
-
-// Chain j of block b is chain index (k * gridDim.x + b) * RFK_BLOCK + tid for
-// k in [0, RFK_CPT). Each block owns one temporal sample (sample = block).
-extern "C" __global__ void __launch_bounds__(RFK_BLOCK) rfk_warmup(const float* __restrict__ samples, rfk_chains st,
-                                                                   unsigned w, unsigned h, unsigned seed, unsigned salt,
-                                                                   unsigned warmup_count,
-                                                                   unsigned long long* __restrict__ warmup_hits) {
-    __shared__ __align__(16) float P[RFK_SAMPLE_FLOATS];
-    __shared__ unsigned long long block_hits;
-    const float* src = samples + (size_t)blockIdx.x * RFK_SAMPLE_FLOATS;
-    for (unsigned i = threadIdx.x; i < RFK_SAMPLE_FLOATS; i += RFK_BLOCK) P[i] = src[i];
-    if (threadIdx.x == 0) block_hits = 0;
-    __syncthreads();
-    const unsigned total = gridDim.x * RFK_BLOCK * RFK_CPT;
-    unsigned long long my_hits = 0;
-#pragma unroll 1
-    for (int k = 0; k < RFK_CPT; k++) {
-        const unsigned chain = (k * gridDim.x + blockIdx.x) * RFK_BLOCK + threadIdx.x;
-        Rng rng;
-        rng.start(chain, 0xFFFDu, 0ull, seed, salt);
-        V2 pos = rfk_hammersley(chain, total);
-        float px = (pos.x + 1.0f) / 2.0f * (float)w;
-        float py = (pos.y + 1.0f) / 2.0f * (float)h;
-        // plane-space affine at P[6..11]
-        float x = fmaf(P[6], px, fmaf(P[8], py, P[10]));
-        float y = fmaf(P[7], px, fmaf(P[9], py, P[11]));
-        float c = rng.u01();
-        unsigned last = 255u;
-#pragma unroll 1
-        for (unsigned pass = 0; pass < warmup_count; pass++) {
-            Rng r2;
-            r2.start(chain, 0xFFFEu, (unsigned long long)pass, seed, salt);
-            float4 contrib;
-            unsigned hit;
-            rfk_step(x, y, c, last, r2, P, w, h, contrib, hit);
-            my_hits += hit;
-        }
-        st.x[chain] = x;
-        st.y[chain] = y;
-        st.c[chain] = c;
-#if RFK_CHAOS
-        st.last[chain] = (unsigned char)last;
-#endif
-    }
-    atomicAdd(&block_hits, my_hits);
-    __syncthreads();
-    if (threadIdx.x == 0) atomicAdd(warmup_hits, block_hits);
 }
 
 // ------------------------------------------------------------------ bin ----
@@ -566,31 +532,138 @@ __device__ __forceinline__ void rfk_rotate(float (&x)[RFK_CPT], float (&y)[RFK_C
     rfk_rot1(last, chain);
 }
 
-extern "C" __global__ void __launch_bounds__(RFK_BLOCK) rfk_bin(rfk_bin_args a) {
+// Shared memory of a block's passes: sort staging and the hot-pixel cache.
+struct rfk_pass_smem {
+#if RFK_SORT == 1
+    float4 stage[RFK_BLOCK / 32][32 * RFK_CPT];
+    unsigned counts[RFK_BLOCK / 32][32];
+#elif RFK_SORT == 2
+    float4 stage[RFK_BLOCK * RFK_CPT];
+    unsigned counts[2][RFK_NX * (RFK_BLOCK / 32)];  // ping-pong sets, one per pass parity
+#endif
+#if RFK_FLUSH >= 2
+    rfk_cache cache;
+#endif
+    unsigned dummy;
+};
+
+// All threads of the block, once, before the first pass.
+__device__ __forceinline__ void rfk_pass_smem_init(rfk_pass_smem& sm) {
+#if RFK_SORT == 2
+    for (unsigned i = threadIdx.x; i < 2 * RFK_NX * (RFK_BLOCK / 32); i += RFK_BLOCK) (&sm.counts[0][0])[i] = 0u;
+#endif
+#if RFK_FLUSH >= 2
+    rfk_cache_clear(sm.cache);
+#endif
+}
+
+#if RFK_FLUSH >= 2
+#define RFK_CACHE_ARG , sm.cache
+#else
+#define RFK_CACHE_ARG
+#endif
+
+// One pass over this thread's RFK_CPT chains, in two parts with the loop over
+// chain slots in the kernel body:
+//   rfk_pick_sort  every thread of the block (the block sort synchronises):
+//                  picks of this lane's chains from one Philox stream per lane
+//                  (lane_stream, call_id, pass), then the sort by xform;
+//   rfk_move_slot  RFK_CPT times: the chain in slot 0 moves (Philox stream of
+//                  the slot, call_id, pass) and draws unless `draw` is false
+//                  (warm-up), then the slots rotate by one. Its pointers carry
+//                  no __restrict__: with it the compiler kept the flame
+//                  parameters in registers across the loop (about 155
+//                  registers per thread instead of 60, a quarter of the
+//                  occupancy).
+// Without sorting (RFK_SORT 0) rfk_pick_sort does nothing and rfk_move_slot
+// picks and moves the chain in slot 0.
+__device__ __forceinline__ void rfk_pick_sort(float (&x)[RFK_CPT], float (&y)[RFK_CPT], float (&c)[RFK_CPT],
+                                              const unsigned (&last)[RFK_CPT], int (&kk)[RFK_CPT], rfk_pass_smem& sm,
+                                              const float* P, unsigned lane_stream, unsigned call_id,
+                                              unsigned long long pass, unsigned seed, unsigned salt) {
+#if RFK_SORT
+    Rng pr;
+    pr.start_lazy(lane_stream, call_id, pass, seed, salt ^ 0x9E3779B9u);
+#pragma unroll
+    for (int k = 0; k < RFK_CPT; k++) kk[k] = rfk_pick(pr.u01(), P, last[k]);
+#if RFK_SORT == 2
+    rfk_block_sort(x, y, c, kk, sm.stage, sm.counts[pass & 1], sm.counts[(pass + 1) & 1]);
+#else
+    rfk_sort_chains(x, y, c, kk, sm.stage[threadIdx.x >> 5], sm.counts[threadIdx.x >> 5]);
+#endif
+#else
+    (void)x; (void)y; (void)c; (void)last; (void)sm; (void)P; (void)lane_stream; (void)call_id; (void)pass;
+    (void)seed; (void)salt;
+#pragma unroll
+    for (int k = 0; k < RFK_CPT; k++) kk[k] = 0;
+#endif
+}
+
+__device__ __forceinline__ void rfk_move_slot(float (&x)[RFK_CPT], float (&y)[RFK_CPT], float (&c)[RFK_CPT],
+                                              int (&kk)[RFK_CPT], unsigned (&last)[RFK_CPT], unsigned (&chain)[RFK_CPT],
+                                              rfk_pass_smem& sm, const float* P, float4* bins,
+                                              unsigned w, unsigned h, unsigned call_id, unsigned long long pass,
+                                              unsigned seed, unsigned salt, bool draw, unsigned& my_hits,
+                                              unsigned& my_draws) {
+    float4 v;
+    unsigned hit;
+    int idx;
+#if RFK_SORT
+#if RFK_CHAOS
+    last[0] = (unsigned)kk[0];
+#endif
+    Rng rng;
+    rng.start_lazy(chain[0], call_id, pass, seed, salt);
+    idx = rfk_move(kk[0], x[0], y[0], c[0], rng, P, w, h, v, hit);
+#else
+    Rng rng;
+    rng.start(chain[0], call_id, pass, seed, salt);
+    idx = rfk_step(x[0], y[0], c[0], last[0], rng, P, w, h, v, hit);
+#endif
+    if (draw) {
+        rfk_flush(bins, idx, v RFK_CACHE_ARG);
+        my_hits += hit;
+        my_draws += (idx >= 0) ? 1u : 0u;
+    }
+    rfk_rotate(x, y, c, kk, last, chain);
+}
+
+// Block totals of the check interval: warp sums, then shared atomics. Ends
+// with a barrier after which s_hits / s_draws hold the block's sums and the
+// hot-pixel cache is flushed.
+__device__ __forceinline__ void rfk_block_totals(unsigned& my_hits, unsigned& my_draws, unsigned long long* s_hits,
+                                                 unsigned long long* s_draws, rfk_pass_smem& sm, float4* bins) {
+    unsigned wh = __reduce_add_sync(0xffffffffu, my_hits);
+    unsigned wd = __reduce_add_sync(0xffffffffu, my_draws);
+    my_hits = 0;
+    my_draws = 0;
+    if ((threadIdx.x & 31u) == 0) {
+        atomicAdd(s_hits, (unsigned long long)wh);
+        atomicAdd(s_draws, (unsigned long long)wd);
+    }
+    __syncthreads();
+#if RFK_FLUSH >= 2
+    rfk_cache_flush(sm.cache, bins);
+#else
+    (void)sm;
+    (void)bins;
+#endif
+}
+
+#ifdef RFK_MINB
+#define RFK_BIN_BOUNDS __launch_bounds__(RFK_BLOCK, RFK_MINB)
+#else
+#define RFK_BIN_BOUNDS __launch_bounds__(RFK_BLOCK)
+#endif
+
+extern "C" __global__ void RFK_BIN_BOUNDS rfk_bin(rfk_bin_args a) {
     __shared__ __align__(16) float P[RFK_SAMPLE_FLOATS];
     __shared__ unsigned long long s_hits, s_draws;
     __shared__ unsigned s_bail;
     __shared__ unsigned long long s_start;
-#if RFK_SORT == 1
-    __shared__ float4 s_stage[RFK_BLOCK / 32][32 * RFK_CPT];
-    __shared__ unsigned s_counts[RFK_BLOCK / 32][32];
-    float4* stage = s_stage[threadIdx.x >> 5];
-    unsigned* counts = s_counts[threadIdx.x >> 5];
-#elif RFK_SORT == 2
-    __shared__ float4 s_stage[RFK_BLOCK * RFK_CPT];
-    __shared__ unsigned s_counts[2][RFK_NX * (RFK_BLOCK / 32)];
-    for (unsigned i = threadIdx.x; i < 2 * RFK_NX * (RFK_BLOCK / 32); i += RFK_BLOCK) (&s_counts[0][0])[i] = 0u;
-#endif
-#if RFK_SORT
+    __shared__ rfk_pass_smem sm;
+    rfk_pass_smem_init(sm);
     const unsigned lane_stream = blockIdx.x * RFK_BLOCK + threadIdx.x;
-#endif
-#if RFK_FLUSH == 2
-    __shared__ rfk_cache cache;
-    rfk_cache_clear(cache);
-#define RFK_CACHE_ARG , cache
-#else
-#define RFK_CACHE_ARG
-#endif
     const float* src = a.samples + (size_t)blockIdx.x * RFK_SAMPLE_FLOATS;
     for (unsigned i = threadIdx.x; i < RFK_SAMPLE_FLOATS; i += RFK_BLOCK) P[i] = src[i];
     if (threadIdx.x == 0) {
@@ -623,64 +696,16 @@ extern "C" __global__ void __launch_bounds__(RFK_BLOCK) rfk_bin(rfk_bin_args a) 
     for (;;) {
 #pragma unroll 1
         for (unsigned it = 0; it < a.check && (a.max_passes == 0 || pass < a.max_passes); it++) {
-#if RFK_SORT
-            // picks of this lane's chains from one Philox stream per lane
-            Rng pr;
-            pr.start_lazy(lane_stream, a.call_id, pass, a.seed, a.salt ^ 0x9E3779B9u);
             int kk[RFK_CPT];
-#pragma unroll
-            for (int k = 0; k < RFK_CPT; k++) kk[k] = rfk_pick(pr.u01(), P, last[k]);
-#if RFK_SORT == 2
-            // ping-pong counter sets, one per pass parity
-            rfk_block_sort(x, y, c, kk, s_stage, s_counts[pass & 1], s_counts[(pass + 1) & 1]);
-#else
-            rfk_sort_chains(x, y, c, kk, stage, counts);
-#endif
-            // One copy of the chain-step code (smaller instruction footprint):
-            // the chain in slot 0 is moved, then the slots rotate by one.
+            rfk_pick_sort(x, y, c, last, kk, sm, P, lane_stream, a.call_id, pass, a.seed, a.salt);
 #pragma unroll 1
-            for (int k = 0; k < RFK_CPT; k++) {
-#if RFK_CHAOS
-                last[0] = (unsigned)kk[0];
-#endif
-                Rng rng;
-                rng.start_lazy(chain[0], a.call_id, pass, a.seed, a.salt);
-                float4 v;
-                unsigned hit;
-                int idx = rfk_move(kk[0], x[0], y[0], c[0], rng, P, a.w, a.h, v, hit);
-                rfk_flush(a.bins, idx, v RFK_CACHE_ARG);
-                my_hits += hit;
-                my_draws += (idx >= 0) ? 1u : 0u;
-                rfk_rotate(x, y, c, kk, last, chain);
-            }
-#else
-#pragma unroll
-            for (int k = 0; k < RFK_CPT; k++) {
-                Rng rng;
-                rng.start(chain[k], a.call_id, pass, a.seed, a.salt);
-                float4 v;
-                unsigned hit;
-                int idx = rfk_step(x[k], y[k], c[k], last[k], rng, P, a.w, a.h, v, hit);
-                rfk_flush(a.bins, idx, v RFK_CACHE_ARG);
-                my_hits += hit;
-                my_draws += (idx >= 0) ? 1u : 0u;
-            }
-#endif
+            for (int k = 0; k < RFK_CPT; k++)
+                rfk_move_slot(x, y, c, kk, last, chain, sm, P, a.bins, a.w, a.h, a.call_id, pass, a.seed, a.salt, true,
+                              my_hits, my_draws);
             pass++;
         }
         // bailout check: block totals -> global counters -> decision
-        unsigned wh = __reduce_add_sync(0xffffffffu, my_hits);
-        unsigned wd = __reduce_add_sync(0xffffffffu, my_draws);
-        my_hits = 0;
-        my_draws = 0;
-        if ((threadIdx.x & 31u) == 0) {
-            atomicAdd(&s_hits, (unsigned long long)wh);
-            atomicAdd(&s_draws, (unsigned long long)wd);
-        }
-        __syncthreads();
-#if RFK_FLUSH == 2
-        rfk_cache_flush(cache, a.bins);
-#endif
+        rfk_block_totals(my_hits, my_draws, &s_hits, &s_draws, sm, a.bins);
         if (threadIdx.x == 0) {
             unsigned long long q = atomicAdd(&a.counters->quality, s_hits) + s_hits;
             atomicAdd(&a.counters->draws, s_draws);
@@ -713,6 +738,257 @@ extern "C" __global__ void __launch_bounds__(RFK_BLOCK) rfk_bin(rfk_bin_args a) 
     if (threadIdx.x == 0) {
         atomicAdd(&a.counters->passes, pass * (unsigned long long)(RFK_BLOCK * RFK_CPT));
         atomicOr(&a.counters->status, s_bail);
+        atomicMax(&a.counters->stop_ns, rfk_time());
+    }
+}
+
+// --------------------------------------------------------------- warmup ----
+// Chain slot k of thread t in block b holds chain (k * gridDim.x + b) *
+// RFK_BLOCK + t. Each block owns one temporal sample (sample = block). Start
+// points: the Hammersley point of the chain over all chains, mapped to pixel
+// space and through the plane-space affine (refactor.cu:301-308), colour
+// ~ U(0,1); then warmup_count passes that move the chains without drawing
+// (refactor.cu:311-335), on the pass code of rfk_bin (Philox sub-stream
+// 0xFFFE, which bin calls never use).
+extern "C" __global__ void RFK_BIN_BOUNDS rfk_warmup(const float* __restrict__ samples, rfk_chains st, unsigned w,
+                                                     unsigned h, unsigned seed, unsigned salt, unsigned warmup_count) {
+    __shared__ __align__(16) float P[RFK_SAMPLE_FLOATS];
+    __shared__ rfk_pass_smem sm;
+    rfk_pass_smem_init(sm);
+    const float* src = samples + (size_t)blockIdx.x * RFK_SAMPLE_FLOATS;
+    for (unsigned i = threadIdx.x; i < RFK_SAMPLE_FLOATS; i += RFK_BLOCK) P[i] = src[i];
+    __syncthreads();
+    const unsigned total = gridDim.x * RFK_BLOCK * RFK_CPT;
+    const unsigned lane_stream = blockIdx.x * RFK_BLOCK + threadIdx.x;
+    float x[RFK_CPT], y[RFK_CPT], c[RFK_CPT];
+    unsigned last[RFK_CPT], chain[RFK_CPT];
+#pragma unroll
+    for (int k = 0; k < RFK_CPT; k++) {
+        chain[k] = (k * gridDim.x + blockIdx.x) * RFK_BLOCK + threadIdx.x;
+        Rng rng;
+        rng.start(chain[k], 0xFFFDu, 0ull, seed, salt);
+        const V2 pos = rfk_hammersley(chain[k], total);
+        const float px = (pos.x + 1.0f) / 2.0f * (float)w;
+        const float py = (pos.y + 1.0f) / 2.0f * (float)h;
+        // plane-space affine at P[6..11]
+        x[k] = fmaf(P[6], px, fmaf(P[8], py, P[10]));
+        y[k] = fmaf(P[7], px, fmaf(P[9], py, P[11]));
+        c[k] = rng.u01();
+        last[k] = 255u;
+    }
+    unsigned no_hits = 0, no_draws = 0;
+#pragma unroll 1
+    for (unsigned pass = 0; pass < warmup_count; pass++) {
+        int kk[RFK_CPT];
+        rfk_pick_sort(x, y, c, last, kk, sm, P, lane_stream, 0xFFFEu, pass, seed, salt);
+#pragma unroll 1
+        for (int k = 0; k < RFK_CPT; k++) {
+            rfk_move_slot(x, y, c, kk, last, chain, sm, P, nullptr, w, h, 0xFFFEu, pass, seed, salt, false, no_hits,
+                          no_draws);
+            // without the histogram updates (asm with a memory clobber) the
+            // compiler would keep the flame parameters in registers across
+            // passes: twice the registers, half the occupancy
+            asm volatile("" ::: "memory");
+        }
+    }
+#pragma unroll
+    for (int k = 0; k < RFK_CPT; k++) {
+        st.x[chain[k]] = x[k];
+        st.y[chain[k]] = y[k];
+        st.c[chain[k]] = c[k];
+#if RFK_CHAOS
+        st.last[chain[k]] = (unsigned char)last[k];
+#endif
+    }
+}
+
+// ------------------------------------------------------------ batch bin ----
+// Many flames or frames (units) of one structure in one persistent launch.
+// The work is a queue of items, each `passes_per_item` passes of one block's
+// chains on one unit; items are numbered unit after unit. A block takes the
+// next item with one atomic, skips it when its unit has reached its quality
+// target, loads the unit's parameter block (with a fresh antialiasing jitter
+// at the start and at every quality check), and keeps its chains when the item is of the unit it just worked on (new
+// chains start uniformly over the image, through the plane-space affine, and
+// run `warmup` passes without drawing). A unit's histogram only sees its own
+// items; quality (the sum of 255 * opacity over draws) counts per unit.
+struct rfk_unit {
+    const float* params;                 // prepared parameter block (no jitter)
+    float4* bins;                        // w x h histogram, row-major
+    unsigned w, h;
+    unsigned long long quality_target;   // per-unit target of the quality sum
+    unsigned long long first_item;       // first queue item of this unit
+    unsigned check;                      // passes between quality checks
+    unsigned pad;
+};
+
+struct rfk_unit_counters {
+    unsigned long long quality;  // sum of (u32)(255 * opacity) over draws
+    unsigned long long draws;
+    unsigned long long passes;   // chain steps, warm-up included
+    unsigned long long items;    // items worked on
+};
+
+struct rfk_batch_args {
+    const rfk_unit* units;
+    rfk_unit_counters* uc;
+    unsigned nunits;
+    unsigned passes_per_item;
+    unsigned long long nitems;
+    unsigned long long* next_item;  // queue head, zero at launch
+    unsigned warmup;                // warm-up passes for new chains
+    unsigned seed, salt;
+    const unsigned* call_id;        // device word: Philox sub-stream of this run
+    unsigned long long time_ns;     // time budget per block (0 = none)
+    const volatile unsigned* stop;  // host-written stop flag (may be null)
+    rfk_counters* counters;         // batch totals: passes, start, stop, status
+};
+
+// Antialiasing jitter ~ gauss(1/3 px) of the screen affine (as each temporal
+// sample of the single-flame path has one), drawn afresh at the start of an
+// item and at every quality check, so that a small unit worked on by few
+// blocks still averages over many jitters. Philox stream (item, 0xFFFF,
+// call_id : block pass), unique per draw.
+__device__ __forceinline__ void rfk_batch_jitter(float* P, const float* __restrict__ base, unsigned long long item,
+                                                 unsigned call_id, unsigned long long pass, unsigned seed,
+                                                 unsigned salt) {
+    Rng jr;
+    jr.start((unsigned)item, 0xFFFFu, ((unsigned long long)call_id << 32) | (unsigned)pass, seed, salt);
+    const V2 j = jr.gauss(1.0f / 3.0f);
+    P[4] = base[4] + j.x;
+    P[5] = base[5] + j.y;
+}
+
+extern "C" __global__ void RFK_BIN_BOUNDS rfk_bin_batch(rfk_batch_args a) {
+    __shared__ __align__(16) float P[RFK_SAMPLE_FLOATS];
+    __shared__ unsigned long long s_hits, s_draws, s_start, s_item;
+    __shared__ int s_unit;
+    __shared__ unsigned s_bail;
+    __shared__ rfk_pass_smem sm;
+    rfk_pass_smem_init(sm);
+    const unsigned lane_stream = blockIdx.x * RFK_BLOCK + threadIdx.x;
+    const unsigned call_id = *a.call_id;
+    if (threadIdx.x == 0) {
+        s_hits = 0;
+        s_draws = 0;
+        s_start = rfk_time();
+        atomicMin(&a.counters->start_ns, s_start);
+    }
+    float x[RFK_CPT], y[RFK_CPT], c[RFK_CPT];
+    unsigned last[RFK_CPT];
+    unsigned chain[RFK_CPT];
+#pragma unroll
+    for (int k = 0; k < RFK_CPT; k++) {
+        chain[k] = (k * gridDim.x + blockIdx.x) * RFK_BLOCK + threadIdx.x;
+        x[k] = y[k] = c[k] = 0.0f;
+        last[k] = 255u;
+    }
+    int cur = -1;
+    unsigned long long pass = 0;  // the block's running pass count
+    unsigned long long total_passes = 0;
+    unsigned status = 0;
+    unsigned my_hits = 0, my_draws = 0;
+#pragma unroll 1
+    for (;;) {
+        __syncthreads();  // everyone is done with the previous item's parameters
+        if (threadIdx.x == 0) {
+            int u = -1;
+            unsigned long long item = 0;
+            unsigned bail = 0;
+            if (a.stop && *a.stop) bail |= RFK_ST_STOP;
+            if (a.time_ns && rfk_time() - s_start >= a.time_ns) bail |= RFK_ST_TIME;
+            while (!bail) {
+                item = atomicAdd(a.next_item, 1ull);
+                if (item >= a.nitems) break;
+                // the unit of the item: the last one whose first item <= item
+                int lo = 0, hi = (int)a.nunits - 1;
+                while (lo < hi) {
+                    const int mid = (lo + hi + 1) >> 1;
+                    if (a.units[mid].first_item <= item) lo = mid;
+                    else hi = mid - 1;
+                }
+                const unsigned long long q = *((volatile unsigned long long*)&a.uc[lo].quality);
+                if (q < a.units[lo].quality_target) {
+                    u = lo;
+                    break;
+                }
+            }
+            status |= bail;
+            s_unit = u;
+            s_item = item;
+        }
+        __syncthreads();
+        const int u = s_unit;
+        if (u < 0) break;
+        const unsigned long long item = s_item;
+        const rfk_unit U = a.units[u];
+        for (unsigned i = threadIdx.x; i < RFK_SAMPLE_FLOATS; i += RFK_BLOCK) P[i] = U.params[i];
+        __syncthreads();
+        if (threadIdx.x == 0) rfk_batch_jitter(P, U.params, item, call_id, pass, a.seed, a.salt);
+        __syncthreads();
+        unsigned warm = 0;
+        if (u != cur) {
+#pragma unroll
+            for (int k = 0; k < RFK_CPT; k++) {
+                Rng r0;
+                r0.start(chain[k], 0xFFFDu, ((unsigned long long)call_id << 32) | (unsigned)item, a.seed, a.salt);
+                const float px = r0.u01() * (float)U.w, py = r0.u01() * (float)U.h;
+                x[k] = fmaf(P[6], px, fmaf(P[8], py, P[10]));
+                y[k] = fmaf(P[7], px, fmaf(P[9], py, P[11]));
+                c[k] = r0.u01();
+                last[k] = 255u;
+            }
+            warm = a.warmup;
+            cur = u;
+        }
+        const unsigned total = warm + a.passes_per_item;
+        unsigned done = 0;
+        unsigned ended = 0;
+#pragma unroll 1
+        while (done < total) {
+            const unsigned n = min(U.check, total - done);
+#pragma unroll 1
+            for (unsigned it = 0; it < n; it++) {
+                const bool draw = done + it >= warm;
+                int kk[RFK_CPT];
+                rfk_pick_sort(x, y, c, last, kk, sm, P, lane_stream, call_id, pass, a.seed, a.salt);
+#pragma unroll 1
+                for (int k = 0; k < RFK_CPT; k++)
+                    rfk_move_slot(x, y, c, kk, last, chain, sm, P, U.bins, U.w, U.h, call_id, pass, a.seed, a.salt, draw,
+                                  my_hits, my_draws);
+                pass++;
+            }
+            done += n;
+            rfk_block_totals(my_hits, my_draws, &s_hits, &s_draws, sm, U.bins);
+            if (threadIdx.x == 0) {
+                const unsigned long long q = atomicAdd(&a.uc[u].quality, s_hits) + s_hits;
+                atomicAdd(&a.uc[u].draws, s_draws);
+                atomicAdd(&a.uc[u].passes, (unsigned long long)n * (RFK_BLOCK * RFK_CPT));
+                s_hits = 0;
+                s_draws = 0;
+                unsigned bail = 0;
+                if (q >= U.quality_target) bail |= RFK_ST_QUALITY;
+                if (a.stop && *a.stop) bail |= RFK_ST_STOP;
+                if (a.time_ns && rfk_time() - s_start >= a.time_ns) bail |= RFK_ST_TIME;
+                s_bail = bail;
+                // a new jitter for the next interval: the other threads wait at
+                // the barrier below and read P only after it
+                if (!bail && done < total) rfk_batch_jitter(P, U.params, item, call_id, pass, a.seed, a.salt);
+            }
+            __syncthreads();
+            ended = s_bail;
+            if (ended) break;
+        }
+        total_passes += done;
+        if (threadIdx.x == 0) atomicAdd(&a.uc[u].items, 1ull);
+        if (ended & (RFK_ST_STOP | RFK_ST_TIME)) {
+            if (threadIdx.x == 0) status |= ended;
+            break;
+        }
+    }
+    if (threadIdx.x == 0) {
+        atomicAdd(&a.counters->passes, total_passes * (unsigned long long)(RFK_BLOCK * RFK_CPT));
+        atomicOr(&a.counters->status, status);
         atomicMax(&a.counters->stop_ns, rfk_time());
     }
 }

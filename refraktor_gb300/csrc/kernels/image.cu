@@ -195,24 +195,25 @@ cudaError_t rfk_launch_catmull(const double* samples, unsigned sample_size, unsi
 
 cudaError_t rfk_launch_tonemap_fast(const float4* bins, unsigned size, void* out, int format, float gamma,
                                     float scale_constant, float brightness, float vibrancy, float highlight_power,
-                                    unsigned long long* hist, unsigned long long* max_density, unsigned blocks,
-                                    cudaStream_t s);
+                                    unsigned long long* hist, unsigned long long* max_density,
+                                    const unsigned long long* q_hits, double q_per_hit, unsigned blocks, cudaStream_t s);
 
 cudaError_t rfk_launch_tonemap(const float4* bins, unsigned size, void* out, int format, int precise, float gamma,
                                float scale_constant, float brightness, float vibrancy, float highlight_power,
-                               unsigned long long* hist, unsigned long long* max_density, cudaStream_t s) {
+                               unsigned long long* hist, unsigned long long* max_density, const unsigned long long* q_hits,
+                               double q_per_hit, cudaStream_t s) {
     if (size == 0) return cudaSuccess;
     unsigned blocks = (size + 255) / 256;
     const unsigned cap = (unsigned)sm_count() * 8;
     if (blocks > cap) blocks = cap;
     if (!precise)
         return rfk_launch_tonemap_fast(bins, size, out, format, gamma, scale_constant, brightness, vibrancy, highlight_power,
-                                       hist, max_density, blocks, s);
+                                       hist, max_density, q_hits, q_per_hit, blocks, s);
     switch (format) {
-    case 0: rfk_tm::launch<true, 3>(blocks, s, bins, out, size, gamma, scale_constant, brightness, vibrancy, highlight_power, hist, max_density); break;
-    case 1: rfk_tm::launch<true, 4>(blocks, s, bins, out, size, gamma, scale_constant, brightness, vibrancy, highlight_power, hist, max_density); break;
-    case 2: rfk_tm::launch<false, 3>(blocks, s, bins, out, size, gamma, scale_constant, brightness, vibrancy, highlight_power, hist, max_density); break;
-    case 3: rfk_tm::launch<false, 4>(blocks, s, bins, out, size, gamma, scale_constant, brightness, vibrancy, highlight_power, hist, max_density); break;
+    case 0: rfk_tm::launch<true, 3>(blocks, s, bins, out, size, gamma, scale_constant, brightness, vibrancy, highlight_power, hist, max_density, q_hits, q_per_hit); break;
+    case 1: rfk_tm::launch<true, 4>(blocks, s, bins, out, size, gamma, scale_constant, brightness, vibrancy, highlight_power, hist, max_density, q_hits, q_per_hit); break;
+    case 2: rfk_tm::launch<false, 3>(blocks, s, bins, out, size, gamma, scale_constant, brightness, vibrancy, highlight_power, hist, max_density, q_hits, q_per_hit); break;
+    case 3: rfk_tm::launch<false, 4>(blocks, s, bins, out, size, gamma, scale_constant, brightness, vibrancy, highlight_power, hist, max_density, q_hits, q_per_hit); break;
     default: return cudaErrorInvalidValue;
     }
     return cudaGetLastError();

@@ -14,9 +14,12 @@ extern "C" {
 #endif
 
 cudaError_t rfk_launch_catmull(const double* samples, unsigned sample_size, unsigned nseg, float4* coeff, cudaStream_t s);
+// q_hits non-null: the quality is *q_hits * q_per_hit, read on the device,
+// and scale_constant is ignored.
 cudaError_t rfk_launch_tonemap(const float4* bins, unsigned size, void* out, int format, int precise, float gamma,
                                float scale_constant, float brightness, float vibrancy, float highlight_power,
-                               unsigned long long* hist, unsigned long long* max_density, cudaStream_t s);
+                               unsigned long long* hist, unsigned long long* max_density, const unsigned long long* q_hits,
+                               double q_per_hit, cudaStream_t s);
 cudaError_t rfk_launch_density_histogram(const float4* bins, unsigned size, unsigned long long* hist,
                                          unsigned long long* max_density, cudaStream_t s);
 cudaError_t rfk_launch_de_blur(const float4* in, float4* out, unsigned w, unsigned h, float max_radius, float min_radius,

@@ -83,13 +83,20 @@ template <int C, bool HALF>
 __global__ void __launch_bounds__(256) tonemap_kernel(const float4* __restrict__ bins, void* __restrict__ out, unsigned size,
                                                       float gamma, float scale_constant, float brightness, float vibrancy,
                                                       float highlight_power, unsigned long long* __restrict__ hist,
-                                                      unsigned long long* __restrict__ max_density) {
+                                                      unsigned long long* __restrict__ max_density,
+                                                      const unsigned long long* __restrict__ q_hits, double q_per_hit) {
     __shared__ unsigned long long sh[RFK_HISTOGRAM_BINS];
     __shared__ unsigned long long smax;
     if (hist) {
         for (int i = threadIdx.x; i < RFK_HISTOGRAM_BINS; i += blockDim.x) sh[i] = 0;
         if (threadIdx.x == 0) smax = 0;
         __syncthreads();
+    }
+    if (q_hits) {
+        // quality from a device counter (batched renders): the host constant
+        // of the single-image path, computed here in single precision
+        const float q = (float)((double)*q_hits * q_per_hit);
+        scale_constant = powf(10.0f, -log10f(q) - 0.5f);
     }
     const float log_div = 4.0f / logf(2.0f);
     const double inv_gamma = 1.0 / (double)gamma;
@@ -153,9 +160,9 @@ __global__ void __launch_bounds__(256) tonemap_kernel(const float4* __restrict__
 template <bool HALF, int C>
 void launch(unsigned blocks, cudaStream_t s, const float4* bins, void* out, unsigned size, float gamma, float scale_constant,
             float brightness, float vibrancy, float highlight_power, unsigned long long* hist,
-            unsigned long long* max_density) {
+            unsigned long long* max_density, const unsigned long long* q_hits, double q_per_hit) {
     tonemap_kernel<C, HALF><<<blocks, 256, 0, s>>>(bins, out, size, gamma, scale_constant, brightness, vibrancy,
-                                                    highlight_power, hist, max_density);
+                                                    highlight_power, hist, max_density, q_hits, q_per_hit);
 }
 
 }  // namespace rfk_tm

@@ -21,7 +21,8 @@ from typing import Optional, Sequence
 import numpy as np
 
 from . import _lib
-from ._lib import Bailout, BinResult, CompileOpts, DEArgs, KernelInfo, RfkError, TonemapArgs, TuneReport, check, lib, text_out
+from ._lib import (Bailout, BatchInfo, BatchOpts, BatchUnit, BinResult, CompileOpts, DEArgs, KernelInfo, RfkError, TonemapArgs,
+                   TuneReport, check, lib, text_out)
 
 DEFAULT_CONFIG = Path(__file__).resolve().parent / "config"
 
@@ -41,6 +42,17 @@ def _dev_ptr(t) -> int:
     if isinstance(t, int):
         return t
     return int(t.data_ptr())
+
+
+def _device_view(ptr: int, shape: tuple, typestr: str):
+    """A torch CUDA tensor viewing library-owned device memory."""
+    import torch
+
+    class _View:
+        __cuda_array_interface__ = {"shape": shape, "typestr": typestr, "data": (ptr, False), "version": 3,
+                                    "strides": None}
+
+    return torch.as_tensor(_View(), device="cuda")
 
 
 class flamedb:
@@ -259,16 +271,8 @@ class saved_state:
 
     def bins(self):
         """The float4 histogram as a torch CUDA tensor (h, w, 4) viewing state memory."""
-        import torch
-
         w, h = self.dims
-        ptr = self.bins_ptr()
-
-        class _View:
-            __cuda_array_interface__ = {"shape": (h, w, 4), "typestr": "<f4", "data": (ptr, False), "version": 3,
-                                        "strides": None}
-
-        return torch.as_tensor(_View(), device="cuda")
+        return _device_view(self.bins_ptr(), (h, w, 4), "<f4")
 
     def wait(self) -> bin_result:
         r = BinResult()
@@ -307,7 +311,7 @@ class flame_compiler:
         return k
 
 
-def autotune(db: flamedb, f: flame, samples: np.ndarray, dims: Sequence[int], passes: int = 32) -> tuple[dict, dict]:
+def autotune(db: flamedb, f: flame, samples: np.ndarray, dims: Sequence[int], passes: int = 256) -> tuple[dict, dict]:
     """Times launch shapes and flush strategies on this flame; returns
     (compile options, report)."""
     s = np.ascontiguousarray(samples, dtype=np.float64)
@@ -361,3 +365,97 @@ def probe_red_v4(nbytes: int, iters: int = 256) -> float:
 
 def sm_count() -> int:
     return lib().rfk_device_sm_count()
+
+
+def align_flames(db: flamedb, flames: Sequence[flame], by_weight: bool = False) -> list[flame]:
+    """Gives the genomes one structure without changing what each renders (the
+    reference interpolator's alignment, src/refraktor/src/refraktor.cpp:117-191,
+    for any number of genomes); returns new flames."""
+    n = len(flames)
+    ins = (C.c_void_p * n)(*[f._h for f in flames])
+    outs = (C.c_void_p * n)()
+    check(lib().rfk_flames_align(db._h, ins, n, 1 if by_weight else 0, outs))
+    return [flame(C.c_void_p(outs[i]), db) for i in range(n)]
+
+
+@dataclass
+class batch_unit:
+    """One flame or frame of a batch: image size, spp target, spline position
+    (segment, t) in the batch's samples, tonemap parameters."""
+    width: int
+    height: int
+    quality: float
+    segment: int = 0
+    t: float = 0.0
+    gamma: float = 4.0
+    brightness: float = 1.0
+    vibrancy: float = 1.0
+    highlight_power: float = -1.0
+
+
+_PIXEL = {HALF3: (3, "<f2"), HALF4: (4, "<f2"), FLOAT3: (3, "<f4"), FLOAT4: (4, "<f4")}
+
+
+class batch:
+    """Many units of one flame structure in one persistent launch, then blur and
+    tonemap per unit, optionally replayed as one CUDA graph. No reference
+    counterpart (the reference renders one flame per flame_kernel::bin)."""
+
+    def __init__(self, kernel: flame_kernel, units: Sequence[batch_unit], nsamples: int, *, passes_per_item: int = 256,
+                 warmup: int = 20, seed: int = 1, millis: int = 0, de: Optional[Sequence[float]] = None,
+                 out_format: int = HALF4, precise_tonemap: bool = True, item_factor: int = 3):
+        self.kernel = kernel
+        self.units = list(units)
+        arr = (BatchUnit * len(self.units))()
+        for i, u in enumerate(self.units):
+            arr[i] = BatchUnit(u.width, u.height, u.quality, u.segment, u.t, u.gamma, u.brightness, u.vibrancy,
+                               u.highlight_power)
+        de = tuple(de) if de else (0.0, 0.0, 0.0)
+        o = BatchOpts(passes_per_item, warmup, seed, millis, de[0], de[1], de[2], out_format, 1 if precise_tonemap else 0,
+                      item_factor)
+        self.out_format = out_format
+        self.nsamples = int(nsamples)
+        h = C.c_void_p()
+        check(lib().rfk_batch_create(kernel._h, arr, len(self.units), nsamples, C.byref(o), C.byref(h)))
+        self._h = h
+
+    def __del__(self):
+        if getattr(self, "_h", None):
+            lib().rfk_batch_destroy(self._h)
+            self._h = None
+
+    def set_samples(self, samples: np.ndarray) -> None:
+        """nsamples packed samples (any shape holding nsamples x (size_reals + 768) doubles)."""
+        s = np.ascontiguousarray(samples, dtype=np.float64)
+        need = self.nsamples * (self.kernel.info["size_reals"] + 768)
+        if s.size != need:
+            raise RfkError(1, f"samples hold {s.size} values; the batch was created for {need}")
+        check(lib().rfk_batch_set_samples(self._h, s.ctypes.data))
+
+    def run(self, use_graph: bool = False, stream=None) -> None:
+        check(lib().rfk_batch_run(self._h, 1 if use_graph else 0, _stream_ptr(stream)))
+
+    def wait(self) -> tuple[bin_result, list[bin_result]]:
+        tot = BinResult()
+        per = (BinResult * len(self.units))()
+        check(lib().rfk_batch_wait(self._h, C.byref(tot), per))
+        return bin_result(**tot.as_dict()), [bin_result(**per[i].as_dict()) for i in range(len(self.units))]
+
+    def bins(self, u: int):
+        U = self.units[u]
+        return _device_view(lib().rfk_batch_bins(self._h, u), (U.height, U.width, 4), "<f4")
+
+    def image(self, u: int):
+        if self.out_format < 0:
+            raise RfkError(1, "batch has no tonemapped images (out_format < 0)")
+        U = self.units[u]
+        ch, ts = _PIXEL[self.out_format]
+        return _device_view(lib().rfk_batch_image(self._h, u), (U.height, U.width, ch), ts)
+
+    def params(self, u: int):
+        return _device_view(lib().rfk_batch_params(self._h, u), (self.kernel.info["sample_floats"],), "<f4")
+
+    def info(self) -> dict:
+        i = BatchInfo()
+        check(lib().rfk_batch_get_info(self._h, C.byref(i)))
+        return {k: getattr(i, k) for k, _ in BatchInfo._fields_}

@@ -16,6 +16,7 @@ with the palette as [h, s, v] triples.
 """
 from __future__ import annotations
 
+import json
 import math
 
 import numpy as np
@@ -174,3 +175,55 @@ def hd_flame(seed: int = 0, n_xforms: int = 8, final: bool = True, var_set: list
         g["final_xform"] = fx
     g["palette"] = palette(rng)
     return g
+
+
+def keyframe_of(g: dict, seed: int) -> dict:
+    """A keyframe with the structure (xforms, variation sets) of `g` and its own
+    affines, xform weights (Dirichlet(1)) and variation weights (U[0, 1])."""
+    rng = np.random.default_rng(seed + 2_000_003)
+    out = json.loads(json.dumps(g))
+    weights = rng.dirichlet(np.ones(len(out["xforms"])))
+    for xf, wt in zip(out["xforms"], weights):
+        xf["weight"] = float(wt)
+        for vl in xf["vchain"]:
+            vl["transform"] = _affine(rng)
+            vl["variations"] = {n: float(rng.uniform(0.0, 1.0)) for n in vl["variations"]}
+    return out
+
+
+def animation_keyframes(db, seed: int, w: int, h: int, n_xforms: int = 6, count: int = 4) -> list[dict]:
+    """`count` keyframes of one structure (n_xforms xforms, 1-3 variations each
+    from the 14-variation set, no final xform), each framed for w x h and
+    passing the visibility rejection."""
+    base = visible_flame(db, lambda s: hd_flame(s, n_xforms=n_xforms, final=False), seed, w, h)
+    keys = [base]
+    j = 1
+    while len(keys) < count:
+        g, cov = frame_on_gpu(db, keyframe_of(base, seed * 1000 + j), w, h, seed=j, with_coverage=True)
+        if cov >= 0.25:
+            keys.append(dict(g, name=f"{base['name']}.key{j}"))
+        j += 1
+        if j > 256:
+            raise RuntimeError("no visible keyframes")
+    return keys
+
+
+HETERO_SIZES = [(256, 256), (512, 512), (1024, 768), (1280, 720), (1920, 1080), (2048, 1152)]
+HETERO_SPP = [64, 256, 1024]
+
+
+def hetero_batch(db, seed: int, count: int = 64) -> list[dict]:
+    """`count` independent flames: resolution uniform over HETERO_SIZES, xform
+    count uniform in 2..12, spp uniform over HETERO_SPP, 1-3 variations per
+    xform from the 14-variation set, no final xform; each framed for its size
+    and passing the visibility rejection. Returns [{"genome", "width",
+    "height", "spp"}]."""
+    rng = np.random.default_rng(seed + 3_000_003)
+    out = []
+    for i in range(count):
+        w, h = HETERO_SIZES[int(rng.integers(0, len(HETERO_SIZES)))]
+        nx = int(rng.integers(2, 13))
+        spp = HETERO_SPP[int(rng.integers(0, len(HETERO_SPP)))]
+        g = visible_flame(db, lambda s, nx=nx: hd_flame(s, n_xforms=nx, final=False), seed * 100 + i, w, h)
+        out.append({"genome": g, "width": w, "height": h, "spp": spp})
+    return out

@@ -298,7 +298,7 @@ def test_hd_render_colour_matches_oracle(db, comp):
         assert d < 1.25 * floor, (c, d, floor)
 
 
-@pytest.mark.parametrize("sort,flush", [(2, 0), (2, 1), (2, 2), (1, 2), (-1, 1)])
+@pytest.mark.parametrize("sort,flush", [(2, 0), (2, 1), (2, 2), (2, 3), (1, 2), (-1, 1)])
 def test_sort_and_flush_variants_agree(db, comp, sort, flush):
     """Every (sort, flush) variant the autotuner may pick renders the same
     flame: exact draw counts under a pass cap, the same density up to
