@@ -1,0 +1,523 @@
+// Tensor-core kernels of the learned denoiser: 3x3 convolutions (stride 1,
+// zero padding 1) of bf16 NHWC activations as implicit GEMMs on tcgen05, with
+// f32 accumulators in TMEM.
+//
+// conv3x3_tc (forward and input-gradient): one CTA computes a tile of 128
+// output pixels (one row segment of one image) x BN output channels.
+//   D[p, n] = sum over taps t and input channels c of A[p + t, c] * W[n, t, c]
+// The K loop runs over (tap, channel block of BK): the A tile of a K block is
+// a TMA box (BK channels x 128 pixels) of the input tensor at the tap's
+// spatial offset - the padding comes from TMA's zero fill outside the image -
+// and the B tile a box (BK x BN) of the weights [cout][9][cin]. Warp 0 (one
+// lane) issues the TMA loads into a ring of shared-memory stages, warp 1 (one
+// lane) issues tcgen05.mma (M 128, N BN, K 16 per instruction) and frees each
+// stage with tcgen05.commit; all four warps then read the accumulator rows
+// from TMEM (warp w owns lanes 32w..32w+31) and apply the epilogue: bias,
+// ReLU, a ReLU-derivative mask, accumulation into the output, bf16 store.
+// The input gradient of a conv is the same kernel on the output gradient with
+// the weights transposed and the taps flipped ([cin][9][cout]).
+//
+// wgrad3x3_tc (weight gradient): dW[n, t, c] = sum over pixels p of
+// dY[p, n] * X[p + t, c], a GEMM with M = cout (padded to 128 by TMA's zero
+// fill), N = BN input channels, K = pixels, both operands K-major: dY and X
+// are first transposed to channel-major (CHW) copies; a K block is 64 pixels
+// of one image row (W a multiple of 64). A TMA box may not start at an x
+// (innermost) coordinate that is not a multiple of 16 bytes, so the tap's
+// column offset dx in {-1, 0, 1} is applied when X is transposed (one copy per
+// dx, zero outside the image) and the box moves only by the row offset dy.
+// CTAs split K and add their partial sums into dW (f32) atomically.
+#include <cuda.h>
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+
+#include <mutex>
+
+#include "tc_ptx.cuh"
+#include "unet_kernels.h"
+
+namespace {
+
+using bf16 = __nv_bfloat16;
+
+// ------------------------------------------------------------------ conv ----
+struct conv_args {
+    int n_img, h, w, tiles_x;
+    int cin, cin_off;  // K channels and their offset in the input tensor
+    int cout;
+    bf16* out;
+    int out_cstride, out_coff;
+    const float* bias;
+    int relu;
+    const bf16* mask;
+    int mask_cstride, mask_coff;
+    int accumulate;
+    int* err;
+};
+
+template <int BK, int BN>
+struct conv_cfg {
+    static constexpr uint32_t A_BYTES = 128u * BK * 2u;
+    static constexpr uint32_t B_BYTES = (uint32_t)BN * BK * 2u;
+    static constexpr uint32_t STAGE_BYTES = A_BYTES + B_BYTES;
+    // BN 256: one CTA per SM, 4 stages; otherwise about 96 KB for two CTAs per SM
+    static constexpr int STAGES = BN == 256 ? 4 : (98304u / STAGE_BYTES > 8 ? 8 : (int)(98304u / STAGE_BYTES));
+    static constexpr uint32_t SMEM = STAGES * STAGE_BYTES + 1024u;
+};
+
+__device__ __forceinline__ void store_bf16x32(bf16* dst, const float (&v)[32]) {
+    uint4* d = reinterpret_cast<uint4*>(dst);
+#pragma unroll
+    for (int q = 0; q < 4; q++) {
+        __nv_bfloat162 h[4];
+#pragma unroll
+        for (int j = 0; j < 4; j++) h[j] = __floats2bfloat162_rn(v[8 * q + 2 * j], v[8 * q + 2 * j + 1]);
+        d[q] = *reinterpret_cast<uint4*>(h);
+    }
+}
+
+__device__ __forceinline__ void load_bf16x32(const bf16* src, float (&v)[32]) {
+    const uint4* s = reinterpret_cast<const uint4*>(src);
+#pragma unroll
+    for (int q = 0; q < 4; q++) {
+        uint4 u = s[q];
+        const __nv_bfloat162* h = reinterpret_cast<const __nv_bfloat162*>(&u);
+#pragma unroll
+        for (int j = 0; j < 4; j++) {
+            float2 f = __bfloat1622float2(h[j]);
+            v[8 * q + 2 * j] = f.x;
+            v[8 * q + 2 * j + 1] = f.y;
+        }
+    }
+}
+
+template <int BK, int BN>
+__global__ void __launch_bounds__(128) conv3x3_tc(const __grid_constant__ CUtensorMap tmA,
+                                                  const __grid_constant__ CUtensorMap tmB, conv_args p) {
+    using C = conv_cfg<BK, BN>;
+    extern __shared__ uint8_t smem_dyn[];
+    uint8_t* base = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_dyn) + 1023) & ~(uintptr_t)1023);
+    __shared__ uint64_t full[C::STAGES], empty[C::STAGES], done;
+    __shared__ uint32_t tmem_base;
+    __shared__ int s_fail;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+
+    const int mt = blockIdx.x;
+    const int xt = mt % p.tiles_x;
+    const int y = (mt / p.tiles_x) % p.h;
+    const int img = mt / (p.tiles_x * p.h);
+    const int x0 = xt * 128;
+    const int n0 = blockIdx.y * BN;
+    const int kpt = p.cin / BK;  // K blocks per tap
+    const int nk = 9 * kpt;
+
+    if (warp == 0) tc::tmem_alloc(&tmem_base, BN);
+    if (threadIdx.x == 32) {
+        for (int s = 0; s < C::STAGES; s++) {
+            tc::mbar_init(&full[s], 1);
+            tc::mbar_init(&empty[s], 1);
+        }
+        tc::mbar_init(&done, 1);
+        s_fail = 0;
+        tc::mbar_fence_init();
+    }
+    tc::fence_before();
+    __syncthreads();
+    tc::fence_after();
+    const uint32_t tmem = tmem_base;
+
+    if (warp == 0 && lane == 0) {
+        // producer: TMA loads into the stage ring
+        int issued = 0;
+        bool ok = true;
+        for (int kb = 0; kb < nk; kb++) {
+            const int s = kb % C::STAGES, r = kb / C::STAGES;
+            if (r > 0 && !tc::mbar_wait(&empty[s], (r - 1) & 1)) {
+                ok = false;
+                break;
+            }
+            const int tap = kb / kpt, cb = kb - tap * kpt;
+            const int dy = tap / 3 - 1, dx = tap % 3 - 1;
+            uint8_t* sa = base + (size_t)s * C::STAGE_BYTES;
+            tc::mbar_expect_tx(&full[s], C::STAGE_BYTES);
+            tc::tma_load_4d(sa, &tmA, &full[s], p.cin_off + cb * BK, x0 + dx, y + dy, img);
+            tc::tma_load_2d(sa + C::A_BYTES, &tmB, &full[s], tap * p.cin + cb * BK, n0);
+            issued++;
+        }
+        if (!ok) {
+            atomicExch(&s_fail, 1);
+            // let the copies in flight land before the CTA exits (bounded)
+            for (int kb = issued - C::STAGES < 0 ? 0 : issued - C::STAGES; kb < issued; kb++)
+                tc::mbar_wait(&full[kb % C::STAGES], (kb / C::STAGES) & 1);
+        }
+    } else if (warp == 1 && lane == 0) {
+        // MMA issuer
+        constexpr uint32_t idesc = tc::idesc_bf16(128, BN);
+        bool ok = true;
+        for (int kb = 0; kb < nk; kb++) {
+            const int s = kb % C::STAGES, r = kb / C::STAGES;
+            if (!tc::mbar_wait(&full[s], r & 1)) {
+                ok = false;
+                break;
+            }
+            tc::fence_after();
+            const uint32_t sa = tc::smem_u32(base + (size_t)s * C::STAGE_BYTES), sb = sa + C::A_BYTES;
+#pragma unroll
+            for (int kk = 0; kk < BK / 16; kk++)
+                tc::mma_bf16(tmem, tc::smem_desc(sa + kk * 32, BK * 2), tc::smem_desc(sb + kk * 32, BK * 2), idesc,
+                             (kb | kk) != 0 ? 1u : 0u);
+            tc::mma_commit(&empty[s]);
+        }
+        tc::mma_commit(&done);
+        if (!ok) atomicExch(&s_fail, 1);
+    }
+    __syncwarp();
+
+    // epilogue: TMEM lane 32 * warp + lane = tile row
+    bool got = tc::mbar_wait(&done, 0);
+    got = __all_sync(0xffffffffu, got);
+    tc::fence_after();
+    if (got) {
+        const int row = warp * 32 + lane;
+        const int x = x0 + row;
+        const bool valid = x < p.w;
+        const size_t pix = ((size_t)img * p.h + y) * p.w + (valid ? x : 0);
+#pragma unroll 1
+        for (int c = 0; c < BN; c += 32) {
+            float v[32];
+            tc::tmem_ld32(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)c, v);
+            const int ch = n0 + c;
+            if (valid && ch < p.cout) {
+                if (p.bias) {
+#pragma unroll
+                    for (int j = 0; j < 32; j++) v[j] += p.bias[ch + j];
+                }
+                if (p.relu) {
+#pragma unroll
+                    for (int j = 0; j < 32; j++) v[j] = fmaxf(v[j], 0.0f);
+                }
+                if (p.mask) {
+                    float m[32];
+                    load_bf16x32(p.mask + pix * p.mask_cstride + p.mask_coff + ch, m);
+#pragma unroll
+                    for (int j = 0; j < 32; j++) v[j] = m[j] > 0.0f ? v[j] : 0.0f;
+                }
+                bf16* dst = p.out + pix * p.out_cstride + p.out_coff + ch;
+                if (p.accumulate) {
+                    float o[32];
+                    load_bf16x32(dst, o);
+#pragma unroll
+                    for (int j = 0; j < 32; j++) v[j] += o[j];
+                }
+                store_bf16x32(dst, v);
+            }
+        }
+    }
+    tc::fence_before();
+    __syncthreads();
+    if (threadIdx.x == 0 && (!got || s_fail)) atomicExch(p.err, 1);
+    if (warp == 0) tc::tmem_dealloc(tmem, BN);
+}
+
+// ----------------------------------------------------------------- wgrad ----
+struct wgrad_args {
+    int n_img, h, w;
+    int cout, cin;
+    int dx;         // tap column offset of this launch (the X copy is shifted by it)
+    int kpc;        // K blocks (64-pixel row segments) per CTA
+    int total_kb;   // all row segments
+    float* dw;      // [cout][9][cin]
+    int* err;
+};
+
+template <int BN>
+struct wgrad_cfg {
+    static constexpr uint32_t A_BYTES = 128u * 64u * 2u;
+    static constexpr uint32_t B_BYTES = (uint32_t)BN * 64u * 2u;
+    static constexpr uint32_t STAGE_BYTES = A_BYTES + B_BYTES;
+    static constexpr int STAGES = BN == 256 ? 4 : (98304u / STAGE_BYTES > 8 ? 8 : (int)(98304u / STAGE_BYTES));
+    static constexpr uint32_t SMEM = STAGES * STAGE_BYTES + 1024u;
+};
+
+// grid: x = K split, y = m tile * (cin / BN) + n tile, z = tap row (dy + 1)
+template <int BN>
+__global__ void __launch_bounds__(128) wgrad3x3_tc(const __grid_constant__ CUtensorMap tmA,
+                                                   const __grid_constant__ CUtensorMap tmB, wgrad_args p) {
+    using C = wgrad_cfg<BN>;
+    extern __shared__ uint8_t smem_dyn[];
+    uint8_t* base = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_dyn) + 1023) & ~(uintptr_t)1023);
+    __shared__ uint64_t full[C::STAGES], empty[C::STAGES], done;
+    __shared__ uint32_t tmem_base;
+    __shared__ int s_fail;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+
+    const int ntiles = p.cin / BN;
+    const int m0 = (blockIdx.y / ntiles) * 128;
+    const int c0 = (blockIdx.y % ntiles) * BN;
+    const int dy = (int)blockIdx.z - 1;
+    const int tap = (dy + 1) * 3 + (p.dx + 1);
+    const int segs_x = p.w / 64;
+    const int kb0 = blockIdx.x * p.kpc;
+    int nk = p.total_kb - kb0;
+    if (nk > p.kpc) nk = p.kpc;
+    if (nk < 0) nk = 0;
+
+    if (warp == 0) tc::tmem_alloc(&tmem_base, BN);
+    if (threadIdx.x == 32) {
+        for (int s = 0; s < C::STAGES; s++) {
+            tc::mbar_init(&full[s], 1);
+            tc::mbar_init(&empty[s], 1);
+        }
+        tc::mbar_init(&done, 1);
+        s_fail = 0;
+        tc::mbar_fence_init();
+    }
+    tc::fence_before();
+    __syncthreads();
+    tc::fence_after();
+    const uint32_t tmem = tmem_base;
+
+    if (warp == 0 && lane == 0) {
+        int issued = 0;
+        bool ok = true;
+        for (int kb = 0; kb < nk; kb++) {
+            const int s = kb % C::STAGES, r = kb / C::STAGES;
+            if (r > 0 && !tc::mbar_wait(&empty[s], (r - 1) & 1)) {
+                ok = false;
+                break;
+            }
+            const int seg = kb0 + kb;
+            const int xs = seg % segs_x;
+            const int yy = (seg / segs_x) % p.h;
+            const int im = seg / (segs_x * p.h);
+            const int p0 = (int)(((size_t)im * p.h + yy) * p.w + (size_t)xs * 64);
+            uint8_t* sa = base + (size_t)s * C::STAGE_BYTES;
+            tc::mbar_expect_tx(&full[s], C::STAGE_BYTES);
+            tc::tma_load_2d(sa, &tmA, &full[s], p0, m0);
+            tc::tma_load_4d(sa + C::A_BYTES, &tmB, &full[s], xs * 64, yy + dy, c0, im);
+            issued++;
+        }
+        if (!ok) {
+            atomicExch(&s_fail, 1);
+            for (int kb = issued - C::STAGES < 0 ? 0 : issued - C::STAGES; kb < issued; kb++)
+                tc::mbar_wait(&full[kb % C::STAGES], (kb / C::STAGES) & 1);
+        }
+    } else if (warp == 1 && lane == 0) {
+        constexpr uint32_t idesc = tc::idesc_bf16(128, BN);
+        bool ok = true;
+        for (int kb = 0; kb < nk; kb++) {
+            const int s = kb % C::STAGES, r = kb / C::STAGES;
+            if (!tc::mbar_wait(&full[s], r & 1)) {
+                ok = false;
+                break;
+            }
+            tc::fence_after();
+            const uint32_t sa = tc::smem_u32(base + (size_t)s * C::STAGE_BYTES), sb = sa + C::A_BYTES;
+#pragma unroll
+            for (int kk = 0; kk < 4; kk++)
+                tc::mma_bf16(tmem, tc::smem_desc(sa + kk * 32, 128), tc::smem_desc(sb + kk * 32, 128), idesc,
+                             (kb | kk) != 0 ? 1u : 0u);
+            tc::mma_commit(&empty[s]);
+        }
+        tc::mma_commit(&done);
+        if (!ok) atomicExch(&s_fail, 1);
+    }
+    __syncwarp();
+
+    bool got = tc::mbar_wait(&done, 0);
+    got = __all_sync(0xffffffffu, got);
+    tc::fence_after();
+    if (got && nk > 0) {
+        const int m = m0 + warp * 32 + lane;
+#pragma unroll 1
+        for (int c = 0; c < BN; c += 32) {
+            float v[32];
+            tc::tmem_ld32(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)c, v);
+            if (m < p.cout) {
+                float* dst = p.dw + ((size_t)m * 9 + tap) * p.cin + c0 + c;
+#pragma unroll
+                for (int j = 0; j < 32; j++) atomicAdd(dst + j, v[j]);
+            }
+        }
+    }
+    tc::fence_before();
+    __syncthreads();
+    if (threadIdx.x == 0 && (!got || s_fail)) atomicExch(p.err, 1);
+    if (warp == 0) tc::tmem_dealloc(tmem, BN);
+}
+
+// ------------------------------------------------------------- tensor maps --
+using encode_fn = CUresult (*)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*, const cuuint64_t*,
+                               const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave, CUtensorMapSwizzle,
+                               CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+encode_fn encoder() {
+    static encode_fn fn = nullptr;
+    static std::once_flag once;
+    std::call_once(once, [] {
+        void* p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = reinterpret_cast<encode_fn>(p);
+    });
+    return fn;
+}
+
+bool make_map(CUtensorMap* m, const void* base, int rank, const cuuint64_t* dims, const cuuint64_t* strides_bytes,
+              const cuuint32_t* box, CUtensorMapSwizzle sw) {
+    encode_fn fn = encoder();
+    if (!fn) return false;
+    cuuint32_t es[4] = {1, 1, 1, 1};
+    return fn(m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, (cuuint32_t)rank, const_cast<void*>(base), dims, strides_bytes, box, es,
+              CU_TENSOR_MAP_INTERLEAVE_NONE, sw, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+              CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
+template <typename K>
+cudaError_t raise_smem(K kernel, uint32_t bytes) {
+    return cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+}
+
+template <int BK, int BN>
+cudaError_t launch_conv(const CUtensorMap& a, const CUtensorMap& b, const conv_args& p, cudaStream_t s) {
+    using C = conv_cfg<BK, BN>;
+    static std::once_flag once;
+    static cudaError_t attr = cudaSuccess;
+    std::call_once(once, [] { attr = raise_smem(conv3x3_tc<BK, BN>, C::SMEM); });
+    if (attr != cudaSuccess) return attr;
+    dim3 grid((unsigned)(p.n_img * p.h * p.tiles_x), (unsigned)(p.cout / BN));
+    conv3x3_tc<BK, BN><<<grid, 128, C::SMEM, s>>>(a, b, p);
+    return cudaGetLastError();
+}
+
+template <int BN>
+cudaError_t launch_wgrad(const CUtensorMap& a, const CUtensorMap& b, const wgrad_args& p, int splits, cudaStream_t s) {
+    using C = wgrad_cfg<BN>;
+    static std::once_flag once;
+    static cudaError_t attr = cudaSuccess;
+    std::call_once(once, [] { attr = raise_smem(wgrad3x3_tc<BN>, C::SMEM); });
+    if (attr != cudaSuccess) return attr;
+    const int mtiles = (p.cout + 127) / 128;
+    dim3 grid((unsigned)splits, (unsigned)(mtiles * (p.cin / BN)), 3u);
+    wgrad3x3_tc<BN><<<grid, 128, C::SMEM, s>>>(a, b, p);
+    return cudaGetLastError();
+}
+
+int pick_bn(int c) {
+    for (int bn : {256, 128, 64, 32})
+        if (c % bn == 0) return bn;
+    return 0;
+}
+
+}  // namespace
+
+extern "C" cudaError_t rfk_unet_conv3x3(const void* in, int n_img, int h, int w, int in_cstride, int in_coff, int cin,
+                                        const void* weights, int cout, const float* bias, int relu, void* out,
+                                        int out_cstride, int out_coff, const void* mask, int mask_cstride, int mask_coff,
+                                        int accumulate, int* err, cudaStream_t s) {
+    if (cin % 32 || in_coff % 32 || in_cstride % 32 || cout % 32 || out_coff % 32 || out_cstride % 32) return cudaErrorInvalidValue;
+    if (mask && (mask_coff % 32 || mask_cstride % 32)) return cudaErrorInvalidValue;
+    if (in_coff + cin > in_cstride || out_coff + cout > out_cstride || n_img <= 0 || h <= 0 || w <= 0)
+        return cudaErrorInvalidValue;
+    if ((reinterpret_cast<uintptr_t>(in) | reinterpret_cast<uintptr_t>(weights) | reinterpret_cast<uintptr_t>(out)) & 63)
+        return cudaErrorMisalignedAddress;
+    const int bk = (cin % 64 == 0 && in_coff % 64 == 0) ? 64 : 32;
+    const int bn = pick_bn(cout);
+    CUtensorMap ma, mb;
+    const CUtensorMapSwizzle sw = bk == 64 ? CU_TENSOR_MAP_SWIZZLE_128B : CU_TENSOR_MAP_SWIZZLE_64B;
+    {
+        cuuint64_t dims[4] = {(cuuint64_t)in_cstride, (cuuint64_t)w, (cuuint64_t)h, (cuuint64_t)n_img};
+        cuuint64_t str[3] = {(cuuint64_t)in_cstride * 2, (cuuint64_t)w * in_cstride * 2, (cuuint64_t)h * w * in_cstride * 2};
+        cuuint32_t box[4] = {(cuuint32_t)bk, 128, 1, 1};
+        if (!make_map(&ma, in, 4, dims, str, box, sw)) return cudaErrorInvalidValue;
+    }
+    {
+        cuuint64_t dims[2] = {(cuuint64_t)9 * cin, (cuuint64_t)cout};
+        cuuint64_t str[1] = {(cuuint64_t)9 * cin * 2};
+        cuuint32_t box[2] = {(cuuint32_t)bk, (cuuint32_t)bn};
+        if (!make_map(&mb, weights, 2, dims, str, box, sw)) return cudaErrorInvalidValue;
+    }
+    conv_args p{};
+    p.n_img = n_img;
+    p.h = h;
+    p.w = w;
+    p.tiles_x = (w + 127) / 128;
+    p.cin = cin;
+    p.cin_off = in_coff;
+    p.cout = cout;
+    p.out = static_cast<bf16*>(out);
+    p.out_cstride = out_cstride;
+    p.out_coff = out_coff;
+    p.bias = bias;
+    p.relu = relu;
+    p.mask = static_cast<const bf16*>(mask);
+    p.mask_cstride = mask_cstride;
+    p.mask_coff = mask_coff;
+    p.accumulate = accumulate;
+    p.err = err;
+    if (bk == 64) {
+        switch (bn) {
+        case 256: return launch_conv<64, 256>(ma, mb, p, s);
+        case 128: return launch_conv<64, 128>(ma, mb, p, s);
+        case 64: return launch_conv<64, 64>(ma, mb, p, s);
+        default: return launch_conv<64, 32>(ma, mb, p, s);
+        }
+    }
+    switch (bn) {
+    case 256: return launch_conv<32, 256>(ma, mb, p, s);
+    case 128: return launch_conv<32, 128>(ma, mb, p, s);
+    case 64: return launch_conv<32, 64>(ma, mb, p, s);
+    default: return launch_conv<32, 32>(ma, mb, p, s);
+    }
+}
+
+extern "C" cudaError_t rfk_unet_wgrad3x3(const void* dyT, const void* const* xT, int n_img, int h, int w, int cout,
+                                         int cin, float* dw, int* err, cudaStream_t s) {
+    if (w % 64 || cin % 32 || cout <= 0 || cout % 8 || n_img <= 0 || h <= 0) return cudaErrorInvalidValue;
+    if (reinterpret_cast<uintptr_t>(dyT) & 63) return cudaErrorMisalignedAddress;
+    for (int d = 0; d < 3; d++)
+        if (reinterpret_cast<uintptr_t>(xT[d]) & 63) return cudaErrorMisalignedAddress;
+    const int bn = pick_bn(cin);
+    const size_t P = (size_t)n_img * h * w;
+    CUtensorMap ma;
+    {
+        cuuint64_t dims[2] = {(cuuint64_t)P, (cuuint64_t)cout};
+        cuuint64_t str[1] = {(cuuint64_t)P * 2};
+        cuuint32_t box[2] = {64, 128};
+        if (!make_map(&ma, dyT, 2, dims, str, box, CU_TENSOR_MAP_SWIZZLE_128B)) return cudaErrorInvalidValue;
+    }
+    wgrad_args p{};
+    p.n_img = n_img;
+    p.h = h;
+    p.w = w;
+    p.cout = cout;
+    p.cin = cin;
+    p.total_kb = (int)(P / 64);
+    // about 8 CTAs per SM over the three launches' taps and tiles
+    const int mtiles = (cout + 127) / 128;
+    const int per_split = 3 * mtiles * (cin / bn);
+    int splits = (152 * 8 / 3 + per_split - 1) / per_split;
+    if (splits > p.total_kb) splits = p.total_kb;
+    if (splits < 1) splits = 1;
+    p.kpc = (p.total_kb + splits - 1) / splits;
+    splits = (p.total_kb + p.kpc - 1) / p.kpc;
+    p.dw = dw;
+    p.err = err;
+    for (int d = 0; d < 3; d++) {
+        CUtensorMap mb;
+        cuuint64_t dims[4] = {(cuuint64_t)w, (cuuint64_t)h, (cuuint64_t)cin, (cuuint64_t)n_img};
+        cuuint64_t str[3] = {(cuuint64_t)w * 2, (cuuint64_t)h * w * 2, (cuuint64_t)cin * h * w * 2};
+        cuuint32_t box[4] = {64, 1, (cuuint32_t)bn, 1};
+        if (!make_map(&mb, xT[d], 4, dims, str, box, CU_TENSOR_MAP_SWIZZLE_128B)) return cudaErrorInvalidValue;
+        p.dx = d - 1;
+        cudaError_t e;
+        switch (bn) {
+        case 256: e = launch_wgrad<256>(ma, mb, p, splits, s); break;
+        case 128: e = launch_wgrad<128>(ma, mb, p, splits, s); break;
+        case 64: e = launch_wgrad<64>(ma, mb, p, splits, s); break;
+        default: e = launch_wgrad<32>(ma, mb, p, splits, s); break;
+        }
+        if (e != cudaSuccess) return e;
+    }
+    return cudaSuccess;
+}
