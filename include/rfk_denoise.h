@@ -1,0 +1,61 @@
+/*
+ * rfk_denoise.h - C ABI of the learned denoiser (librfk.so).
+ *
+ * Stands in for the reference's denoiser plug-in interface
+ * (src/librefrakt/include/librefrakt/interface/denoiser.h:21-39:
+ * denoiser::make(name, dims, flags, stream) and denoise(in, out, event) ->
+ * future<double ms>), whose implementations wrap closed libraries. This one is
+ * a 4-level BF16 U-Net (32 / 64 / 128 / 256 channels, 3x3 convolutions, ReLU)
+ * on hand-written tcgen05 kernels; it reads the float4 histogram of a
+ * low-spp render (density, colour, alpha, spp as input channels) and writes
+ * the tonemapped image of a converged render. Training (forward, backward,
+ * Adam) runs on the device through the same kernels. Conventions as rfk.h:
+ * rfk_status results, rfk_last_error(), device pointers, void* streams.
+ */
+#ifndef RFK_DENOISE_H
+#define RFK_DENOISE_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#include "rfk.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct rfk_denoiser rfk_denoiser;
+
+/* A network with seeded He-initialised weights. */
+rfk_status rfk_denoiser_create(uint64_t seed, rfk_denoiser** out);
+void rfk_denoiser_destroy(rfk_denoiser* d);
+/* Parameters: per layer the f32 weights [cout][9][cin] then the biases [cout] (host arrays). */
+size_t rfk_denoiser_param_count(const rfk_denoiser* d);
+rfk_status rfk_denoiser_get_params(const rfk_denoiser* d, float* out, size_t n);
+rfk_status rfk_denoiser_set_params(rfk_denoiser* d, const float* in, size_t n);
+
+/* Network input of one w x h float4 histogram rendered at spp: 32 bf16 channels per pixel (device). */
+rfk_status rfk_denoiser_features(const float* bins, uint32_t w, uint32_t h, double spp, void* out, void* stream);
+
+/* One Adam step (learning rate lr) on n histograms (n x h x w float4, device) rendered at spp
+ * against n x h x w RGBA f32 targets (device); *loss = mean squared error of RGB before the step.
+ * w must be a multiple of 512 and h of 8. */
+rfk_status rfk_denoiser_train_step(rfk_denoiser* d, const float* bins, uint32_t n, uint32_t w, uint32_t h, double spp,
+                                   const float* targets, float lr, double* loss, void* stream);
+/* The loss without a step (validation); w and h multiples of 8. */
+rfk_status rfk_denoiser_loss(rfk_denoiser* d, const float* bins, uint32_t n, uint32_t w, uint32_t h, double spp,
+                             const float* targets, double* loss, void* stream);
+/* Parameter gradients of the loss (host array in the parameter layout), without a step. */
+rfk_status rfk_denoiser_gradients(rfk_denoiser* d, const float* bins, uint32_t n, uint32_t w, uint32_t h, double spp,
+                                  const float* targets, float* grads, size_t count, void* stream);
+
+/* denoiser::denoise: the w x h histogram of a render at spp in, the denoised image out in one of
+ * RFK_HALF3 / RFK_HALF4 / RFK_FLOAT3 / RFK_FLOAT4 (alpha as the tonemapper's). w and h multiples of 8. */
+rfk_status rfk_denoise(rfk_denoiser* d, const float* bins, uint32_t w, uint32_t h, double spp, void* out, int format,
+                       void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* RFK_DENOISE_H */

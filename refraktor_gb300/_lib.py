@@ -130,6 +130,21 @@ SIGNATURES = {
     "rfk_batch_image": (C.c_void_p, [C.c_void_p, C.c_size_t]),
     "rfk_batch_params": (C.c_void_p, [C.c_void_p, C.c_size_t]),
     "rfk_batch_get_info": (C.c_int, [C.c_void_p, C.POINTER(BatchInfo)]),
+    # rfk_denoise.h
+    "rfk_denoiser_create": (C.c_int, [C.c_uint64, C.POINTER(C.c_void_p)]),
+    "rfk_denoiser_destroy": (None, [C.c_void_p]),
+    "rfk_denoiser_param_count": (C.c_size_t, [C.c_void_p]),
+    "rfk_denoiser_get_params": (C.c_int, [C.c_void_p, C.c_void_p, C.c_size_t]),
+    "rfk_denoiser_set_params": (C.c_int, [C.c_void_p, C.c_void_p, C.c_size_t]),
+    "rfk_denoiser_features": (C.c_int, [C.c_void_p, C.c_uint32, C.c_uint32, C.c_double, C.c_void_p, C.c_void_p]),
+    "rfk_denoiser_train_step": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint32, C.c_uint32, C.c_uint32, C.c_double,
+                                          C.c_void_p, C.c_float, C.POINTER(C.c_double), C.c_void_p]),
+    "rfk_denoiser_loss": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint32, C.c_uint32, C.c_uint32, C.c_double, C.c_void_p,
+                                    C.POINTER(C.c_double), C.c_void_p]),
+    "rfk_denoiser_gradients": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint32, C.c_uint32, C.c_uint32, C.c_double,
+                                         C.c_void_p, C.c_void_p, C.c_size_t, C.c_void_p]),
+    "rfk_denoise": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint32, C.c_uint32, C.c_double, C.c_void_p, C.c_int,
+                              C.c_void_p]),
 }
 
 

@@ -1,5 +1,6 @@
 // Memory-bound layers of the denoiser around the tensor-core convolutions.
 #include <cuda_bf16.h>
+#include <cuda_fp16.h>
 #include <cuda_runtime.h>
 
 #include "unet_kernels.h"
@@ -36,5 +37,305 @@ extern "C" cudaError_t rfk_unet_to_chw(const void* in, int n_img, int h, int w, 
     dim3 grid((unsigned)((w + 31) / 32), (unsigned)(n_img * h), (unsigned)((c + 31) / 32));
     to_chw_kernel<<<grid, dim3(32, 8), 0, s>>>(static_cast<const bf16*>(in), h, w, cstride, coff, c, dx,
                                                static_cast<bf16*>(out));
+    return cudaGetLastError();
+}
+
+// ------------------------------------------------------------- the rest ----
+namespace {
+
+__device__ __forceinline__ float bf(const bf16 v) { return __bfloat162float(v); }
+
+// Denoiser input of one histogram: 32 bf16 channels per pixel,
+//   0: log1p(density) / 8            1-3: mean colour (rgb / density)
+//   4: alpha, sat(ln(density) * 4 / ln 2 / 96) as the tonemapper's
+//   5: ln(spp) / 8                   6-31: 0
+__global__ void features_kernel(const float4* __restrict__ bins, size_t npx, float spp, bf16* __restrict__ out) {
+    const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= npx) return;
+    const float4 b = bins[i];
+    float f[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+    const float d = b.w;
+    f[0] = log1pf(fmaxf(d, 0.0f)) * 0.125f;
+    if (d > 0.0f) {
+        f[1] = b.x / d;
+        f[2] = b.y / d;
+        f[3] = b.z / d;
+    }
+    f[4] = d >= 1.0f ? fminf(fmaxf(logf(d) * (4.0f / 0.69314718f) / 96.0f, 0.0f), 1.0f) : 0.0f;
+    f[5] = logf(fmaxf(spp, 1.0f)) * 0.125f;
+    __nv_bfloat162 h[16];
+#pragma unroll
+    for (int j = 0; j < 4; j++) h[j] = __floats2bfloat162_rn(f[2 * j], f[2 * j + 1]);
+#pragma unroll
+    for (int j = 4; j < 16; j++) h[j] = __floats2bfloat162_rn(0.0f, 0.0f);
+    uint4* o = reinterpret_cast<uint4*>(out + i * 32);
+#pragma unroll
+    for (int q = 0; q < 4; q++) o[q] = reinterpret_cast<uint4*>(h)[q];
+}
+
+// 2x2 average pool of a channel slice: out[n][y][x][c] = mean of in[n][2y..2y+1][2x..2x+1][coff + c].
+__global__ void avgpool_kernel(const bf16* __restrict__ in, int h, int w, int cstride, int coff, int c,
+                               bf16* __restrict__ out, size_t total) {
+    const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= total) return;
+    const int ch = (int)(i % c);
+    size_t r = i / c;
+    const int ho = h / 2, wo = w / 2;
+    const int x = (int)(r % wo);
+    r /= wo;
+    const int y = (int)(r % ho);
+    const size_t n = r / ho;
+    const size_t b = ((n * h + 2 * y) * w + 2 * x) * cstride + coff + ch;
+    const float s = bf(in[b]) + bf(in[b + cstride]) + bf(in[b + (size_t)w * cstride]) + bf(in[b + (size_t)w * cstride + cstride]);
+    out[i] = __float2bfloat16(0.25f * s);
+}
+
+// Nearest 2x upsample into a channel slice: out[n][y][x][coff + c] = in[n][y / 2][x / 2][c].
+__global__ void upsample_kernel(const bf16* __restrict__ in, int h, int w, int c, bf16* __restrict__ out, int cstride,
+                                int coff, size_t total) {
+    const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= total) return;
+    const int ch = (int)(i % c);
+    size_t r = i / c;
+    const int W = 2 * w, H = 2 * h;
+    const int x = (int)(r % W);
+    r /= W;
+    const int y = (int)(r % H);
+    const size_t n = r / H;
+    out[((n * H + y) * W + x) * cstride + coff + ch] = in[((n * h + y / 2) * w + x / 2) * c + ch];
+}
+
+// Gradient through a nearest 2x upsample (sum of the 2x2 block of a channel
+// slice of g), times the ReLU derivative of the upsampled activation:
+// out[n][y][x][c] = (act > 0) * sum g[n][2y..][2x..][gcoff + c].
+__global__ void up_backward_kernel(const bf16* __restrict__ g, int gcstride, int gcoff, const bf16* __restrict__ act,
+                                   int h, int w, int c, bf16* __restrict__ out, size_t total) {
+    const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= total) return;
+    const int ch = (int)(i % c);
+    size_t r = i / c;
+    const int x = (int)(r % w);
+    r /= w;
+    const int y = (int)(r % h);
+    const size_t n = r / h;
+    const int W = 2 * w;
+    const size_t b = ((n * 2 * h + 2 * y) * W + 2 * x) * gcstride + gcoff + ch;
+    const float s = bf(g[b]) + bf(g[b + gcstride]) + bf(g[b + (size_t)W * gcstride]) + bf(g[b + (size_t)W * gcstride + gcstride]);
+    out[i] = __float2bfloat16(bf(act[i]) > 0.0f ? s : 0.0f);
+}
+
+// Gradient of a skip activation s (a channel slice of a concatenation) that
+// feeds both the concatenation and a 2x2 average pool, times its ReLU
+// derivative: out = (s > 0) * (gcat[slice] + gpool[y / 2][x / 2] / 4).
+__global__ void skip_backward_kernel(const bf16* __restrict__ gcat, int cstride, int coff, const bf16* __restrict__ gpool,
+                                     const bf16* __restrict__ cat, int h, int w, int c, bf16* __restrict__ out,
+                                     size_t total) {
+    const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= total) return;
+    const int ch = (int)(i % c);
+    size_t r = i / c;
+    const int x = (int)(r % w);
+    r /= w;
+    const int y = (int)(r % h);
+    const size_t n = r / h;
+    const size_t px = (n * h + y) * w + x;
+    const float s = bf(cat[px * cstride + coff + ch]);
+    const float gp = bf(gpool[((n * (h / 2) + y / 2) * (w / 2) + x / 2) * c + ch]);
+    const float v = bf(gcat[px * cstride + coff + ch]) + 0.25f * gp;
+    out[i] = __float2bfloat16(s > 0.0f ? v : 0.0f);
+}
+
+// Mean squared error of channels 0..2 of out (f32, cstride 32) against
+// target (f32, 4 per pixel), and its gradient as bf16 (channels 3..31 zero).
+__global__ void mse_kernel(const float* __restrict__ out, const float4* __restrict__ target, size_t npx, float inv_n,
+                           bf16* __restrict__ grad, double* __restrict__ loss) {
+    const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    float l = 0.0f;
+    if (i < npx) {
+        const float4 t = target[i];
+        const float* o = out + i * 32;
+        const float d0 = o[0] - t.x, d1 = o[1] - t.y, d2 = o[2] - t.z;
+        l = d0 * d0 + d1 * d1 + d2 * d2;
+        __nv_bfloat162 hh[16];
+        hh[0] = __floats2bfloat162_rn(2.0f * d0 * inv_n, 2.0f * d1 * inv_n);
+        hh[1] = __floats2bfloat162_rn(2.0f * d2 * inv_n, 0.0f);
+#pragma unroll
+        for (int j = 2; j < 16; j++) hh[j] = __floats2bfloat162_rn(0.0f, 0.0f);
+        uint4* g = reinterpret_cast<uint4*>(grad + i * 32);
+#pragma unroll
+        for (int q = 0; q < 4; q++) g[q] = reinterpret_cast<uint4*>(hh)[q];
+    }
+    for (int o = 16; o; o >>= 1) l += __shfl_xor_sync(0xffffffffu, l, o);
+    if ((threadIdx.x & 31) == 0 && l != 0.0f) atomicAdd(loss, (double)l);
+}
+
+// Per-channel sum over pixels (bias gradient): db[c] += sum_p g[p][c].
+__global__ void bias_grad_kernel(const bf16* __restrict__ g, size_t npx, int c, float* __restrict__ db) {
+    // block: 256 threads = 8 pixel lanes x 32 channels (a channel group of 32)
+    const int cg = blockIdx.y * 32 + (threadIdx.x & 31);
+    const int lanep = threadIdx.x >> 5;
+    float s = 0.0f;
+    for (size_t p = (size_t)blockIdx.x * 8 + lanep; p < npx; p += (size_t)gridDim.x * 8) s += bf(g[p * c + cg]);
+    __shared__ float red[8][32];
+    red[lanep][threadIdx.x & 31] = s;
+    __syncthreads();
+    if (threadIdx.x < 32) {
+        float t = 0.0f;
+        for (int k = 0; k < 8; k++) t += red[k][threadIdx.x];
+        atomicAdd(db + blockIdx.y * 32 + threadIdx.x, t);
+    }
+}
+
+// Adam (Kingma & Ba 2015) on one conv layer's f32 master weights [cout][9][cin]
+// and bias; writes the bf16 copies used by the forward ([cout][9][cin]) and
+// input-gradient ([cin][8 - t][cout]) convolutions. Rows / columns outside
+// (live_out, live_in) stay zero (padded channels of the first and last layer).
+__global__ void adam_kernel(float* __restrict__ w, float* __restrict__ m, float* __restrict__ v,
+                            const float* __restrict__ g, int cout, int cin, int live_out, int live_in, float lr, float b1,
+                            float b2, float eps, float c1, float c2, bf16* __restrict__ wf, bf16* __restrict__ wb) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int n = cout * 9 * cin;
+    if (i >= n) return;
+    const int ci = i % cin, t = (i / cin) % 9, co = i / (9 * cin);
+    float wi = w[i];
+    if (co < live_out && ci < live_in) {
+        const float gi = g[i];
+        const float mi = b1 * m[i] + (1.0f - b1) * gi;
+        const float vi = b2 * v[i] + (1.0f - b2) * gi * gi;
+        m[i] = mi;
+        v[i] = vi;
+        wi -= lr * (mi / c1) / (sqrtf(vi / c2) + eps);
+        w[i] = wi;
+    } else {
+        wi = 0.0f;
+    }
+    const bf16 h = __float2bfloat16(wi);
+    wf[i] = h;
+    wb[((size_t)ci * 9 + (8 - t)) * cout + co] = h;
+}
+
+__global__ void adam_bias_kernel(float* __restrict__ b, float* __restrict__ m, float* __restrict__ v,
+                                 const float* __restrict__ g, int n, int live, float lr, float b1, float b2, float eps,
+                                 float c1, float c2) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    if (i >= live) {
+        b[i] = 0.0f;
+        return;
+    }
+    const float gi = g[i];
+    const float mi = b1 * m[i] + (1.0f - b1) * gi;
+    const float vi = b2 * v[i] + (1.0f - b2) * gi * gi;
+    m[i] = mi;
+    v[i] = vi;
+    b[i] -= lr * (mi / c1) / (sqrtf(vi / c2) + eps);
+}
+
+// Network output (f32, 32 channels, 0..2 used) to an image in the
+// tonemapper's formats; alpha from the histogram as the tonemapper's.
+template <int CH, bool HALF>
+__global__ void to_image_kernel(const float* __restrict__ net, const float4* __restrict__ bins, size_t npx, void* out) {
+    const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= npx) return;
+    const float* o = net + i * 32;
+    float v[4] = {fminf(fmaxf(o[0], 0.0f), 1.0f), fminf(fmaxf(o[1], 0.0f), 1.0f), fminf(fmaxf(o[2], 0.0f), 1.0f), 0.0f};
+    if (CH == 4) {
+        const float d = bins[i].w;
+        v[3] = d > 0.0f ? fminf(fmaxf(logf(d) * (4.0f / 0.69314718f) / 96.0f, 0.0f), 1.0f) : 0.0f;
+    }
+    if (HALF) {
+        __half* h = static_cast<__half*>(out) + i * CH;
+        for (int j = 0; j < CH; j++) h[j] = __float2half_rn(v[j]);
+    } else {
+        float* f = static_cast<float*>(out) + i * CH;
+        for (int j = 0; j < CH; j++) f[j] = v[j];
+    }
+}
+
+inline unsigned blocks_for(size_t n, unsigned t = 256) { return (unsigned)((n + t - 1) / t); }
+
+}  // namespace
+
+extern "C" cudaError_t rfk_unet_features(const float4* bins, size_t npx, float spp, void* out, cudaStream_t s) {
+    if (npx == 0) return cudaSuccess;
+    features_kernel<<<blocks_for(npx), 256, 0, s>>>(bins, npx, spp, static_cast<bf16*>(out));
+    return cudaGetLastError();
+}
+
+extern "C" cudaError_t rfk_unet_avgpool(const void* in, int n_img, int h, int w, int cstride, int coff, int c, void* out,
+                                        cudaStream_t s) {
+    const size_t total = (size_t)n_img * (h / 2) * (w / 2) * c;
+    if (h % 2 || w % 2 || total == 0) return cudaErrorInvalidValue;
+    avgpool_kernel<<<blocks_for(total), 256, 0, s>>>(static_cast<const bf16*>(in), h, w, cstride, coff, c,
+                                                      static_cast<bf16*>(out), total);
+    return cudaGetLastError();
+}
+
+extern "C" cudaError_t rfk_unet_upsample(const void* in, int n_img, int h, int w, int c, void* out, int cstride, int coff,
+                                         cudaStream_t s) {
+    const size_t total = (size_t)n_img * 4 * h * w * c;
+    if (total == 0) return cudaErrorInvalidValue;
+    upsample_kernel<<<blocks_for(total), 256, 0, s>>>(static_cast<const bf16*>(in), h, w, c, static_cast<bf16*>(out),
+                                                       cstride, coff, total);
+    return cudaGetLastError();
+}
+
+extern "C" cudaError_t rfk_unet_up_backward(const void* g, int gcstride, int gcoff, const void* act, int n_img, int h, int w,
+                                            int c, void* out, cudaStream_t s) {
+    const size_t total = (size_t)n_img * h * w * c;
+    if (total == 0) return cudaErrorInvalidValue;
+    up_backward_kernel<<<blocks_for(total), 256, 0, s>>>(static_cast<const bf16*>(g), gcstride, gcoff,
+                                                          static_cast<const bf16*>(act), h, w, c, static_cast<bf16*>(out),
+                                                          total);
+    return cudaGetLastError();
+}
+
+extern "C" cudaError_t rfk_unet_skip_backward(const void* gcat, int cstride, int coff, const void* gpool, const void* cat,
+                                              int n_img, int h, int w, int c, void* out, cudaStream_t s) {
+    const size_t total = (size_t)n_img * h * w * c;
+    if (total == 0 || h % 2 || w % 2) return cudaErrorInvalidValue;
+    skip_backward_kernel<<<blocks_for(total), 256, 0, s>>>(static_cast<const bf16*>(gcat), cstride, coff,
+                                                            static_cast<const bf16*>(gpool), static_cast<const bf16*>(cat),
+                                                            h, w, c, static_cast<bf16*>(out), total);
+    return cudaGetLastError();
+}
+
+extern "C" cudaError_t rfk_unet_mse(const float* out, const float4* target, size_t npx, void* grad, double* loss,
+                                    cudaStream_t s) {
+    if (npx == 0) return cudaSuccess;
+    mse_kernel<<<blocks_for(npx), 256, 0, s>>>(out, target, npx, 1.0f / (3.0f * (float)npx), static_cast<bf16*>(grad),
+                                                loss);
+    return cudaGetLastError();
+}
+
+extern "C" cudaError_t rfk_unet_bias_grad(const void* g, size_t npx, int c, float* db, cudaStream_t s) {
+    if (c % 32 || npx == 0) return cudaErrorInvalidValue;
+    unsigned bx = (unsigned)((npx + 8 * 256 - 1) / (8 * 256));
+    if (bx > 1024) bx = 1024;
+    bias_grad_kernel<<<dim3(bx, (unsigned)(c / 32)), 256, 0, s>>>(static_cast<const bf16*>(g), npx, c, db);
+    return cudaGetLastError();
+}
+
+extern "C" cudaError_t rfk_unet_adam(float* w, float* m, float* v, const float* g, int cout, int cin, int live_out,
+                                     int live_in, float lr, float b1, float b2, float eps, int step, void* wf, void* wb,
+                                     float* bias, float* bm, float* bv, const float* bg, cudaStream_t s) {
+    const float c1 = 1.0f - powf(b1, (float)step), c2 = 1.0f - powf(b2, (float)step);
+    const int n = cout * 9 * cin;
+    adam_kernel<<<blocks_for((size_t)n), 256, 0, s>>>(w, m, v, g, cout, cin, live_out, live_in, lr, b1, b2, eps, c1, c2,
+                                                       static_cast<bf16*>(wf), static_cast<bf16*>(wb));
+    adam_bias_kernel<<<blocks_for((size_t)cout), 256, 0, s>>>(bias, bm, bv, bg, cout, live_out, lr, b1, b2, eps, c1, c2);
+    return cudaGetLastError();
+}
+
+extern "C" cudaError_t rfk_unet_to_image(const float* net, const float4* bins, size_t npx, void* out, int format,
+                                         cudaStream_t s) {
+    if (npx == 0) return cudaSuccess;
+    switch (format) {
+    case 0: to_image_kernel<3, true><<<blocks_for(npx), 256, 0, s>>>(net, bins, npx, out); break;
+    case 1: to_image_kernel<4, true><<<blocks_for(npx), 256, 0, s>>>(net, bins, npx, out); break;
+    case 2: to_image_kernel<3, false><<<blocks_for(npx), 256, 0, s>>>(net, bins, npx, out); break;
+    case 3: to_image_kernel<4, false><<<blocks_for(npx), 256, 0, s>>>(net, bins, npx, out); break;
+    default: return cudaErrorInvalidValue;
+    }
     return cudaGetLastError();
 }

@@ -44,10 +44,11 @@ struct conv_args {
     int n_img, h, w, tiles_x;
     int cin, cin_off;  // K channels and their offset in the input tensor
     int cout;
-    bf16* out;
+    void* out;
     int out_cstride, out_coff;
     const float* bias;
     int relu;
+    int out_f32;  // store f32 instead of bf16
     const bf16* mask;
     int mask_cstride, mask_coff;
     int accumulate;
@@ -201,14 +202,24 @@ __global__ void __launch_bounds__(128) conv3x3_tc(const __grid_constant__ CUtens
 #pragma unroll
                     for (int j = 0; j < 32; j++) v[j] = m[j] > 0.0f ? v[j] : 0.0f;
                 }
-                bf16* dst = p.out + pix * p.out_cstride + p.out_coff + ch;
-                if (p.accumulate) {
-                    float o[32];
-                    load_bf16x32(dst, o);
+                const size_t at = pix * p.out_cstride + p.out_coff + ch;
+                if (p.out_f32) {
+                    float4* dst = reinterpret_cast<float4*>(static_cast<float*>(p.out) + at);
 #pragma unroll
-                    for (int j = 0; j < 32; j++) v[j] += o[j];
+                    for (int q = 0; q < 8; q++) {
+                        float4 o = p.accumulate ? dst[q] : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+                        dst[q] = make_float4(v[4 * q] + o.x, v[4 * q + 1] + o.y, v[4 * q + 2] + o.z, v[4 * q + 3] + o.w);
+                    }
+                } else {
+                    bf16* dst = static_cast<bf16*>(p.out) + at;
+                    if (p.accumulate) {
+                        float o[32];
+                        load_bf16x32(dst, o);
+#pragma unroll
+                        for (int j = 0; j < 32; j++) v[j] += o[j];
+                    }
+                    store_bf16x32(dst, v);
                 }
-                store_bf16x32(dst, v);
             }
         }
     }
@@ -412,7 +423,7 @@ int pick_bn(int c) {
 }  // namespace
 
 extern "C" cudaError_t rfk_unet_conv3x3(const void* in, int n_img, int h, int w, int in_cstride, int in_coff, int cin,
-                                        const void* weights, int cout, const float* bias, int relu, void* out,
+                                        const void* weights, int cout, const float* bias, int flags, void* out,
                                         int out_cstride, int out_coff, const void* mask, int mask_cstride, int mask_coff,
                                         int accumulate, int* err, cudaStream_t s) {
     if (cin % 32 || in_coff % 32 || in_cstride % 32 || cout % 32 || out_coff % 32 || out_cstride % 32) return cudaErrorInvalidValue;
@@ -445,11 +456,12 @@ extern "C" cudaError_t rfk_unet_conv3x3(const void* in, int n_img, int h, int w,
     p.cin = cin;
     p.cin_off = in_coff;
     p.cout = cout;
-    p.out = static_cast<bf16*>(out);
+    p.out = out;
     p.out_cstride = out_cstride;
     p.out_coff = out_coff;
     p.bias = bias;
-    p.relu = relu;
+    p.relu = flags & RFK_UNET_RELU;
+    p.out_f32 = (flags & RFK_UNET_F32OUT) ? 1 : 0;
     p.mask = static_cast<const bf16*>(mask);
     p.mask_cstride = mask_cstride;
     p.mask_coff = mask_coff;

@@ -1,4 +1,4 @@
-"""CPU checks of librfk: it loads, exports every symbol of include/rfk.h, and
+"""CPU checks of librfk: it loads, exports every symbol of include/*.h, and
 its host logic (database, DSL translation, genome layout, codegen, NVRTC
 compile for sm_103a) works without a device."""
 import ctypes
@@ -20,9 +20,11 @@ ROOT = Path(__file__).resolve().parent.parent
 
 
 def header_symbols():
-    text = (ROOT / "include" / "rfk.h").read_text()
     decl = re.compile(r"^(?:const\s+)?[a-z_0-9]+\s*\*?\s*(rfk_[a-z0-9_]+)\s*\(", re.M)
-    return sorted(set(decl.findall(text)))
+    syms = set()
+    for h in sorted((ROOT / "include").glob("*.h")):
+        syms |= set(decl.findall(h.read_text()))
+    return sorted(syms)
 
 
 def test_exports_every_declared_symbol():
