@@ -34,25 +34,28 @@ size_t rfk_denoiser_param_count(const rfk_denoiser* d);
 rfk_status rfk_denoiser_get_params(const rfk_denoiser* d, float* out, size_t n);
 rfk_status rfk_denoiser_set_params(rfk_denoiser* d, const float* in, size_t n);
 
-/* Network input of one w x h float4 histogram rendered at spp: 32 bf16 channels per pixel (device). */
-rfk_status rfk_denoiser_features(const float* bins, uint32_t w, uint32_t h, double spp, void* out, void* stream);
+/* Network input of one w x h float4 histogram rendered at spp and its tonemapped image (float4):
+ * 32 bf16 channels per pixel (device). */
+rfk_status rfk_denoiser_features(const float* bins, const float* base, uint32_t w, uint32_t h, double spp, void* out,
+                                 void* stream);
 
-/* One Adam step (learning rate lr) on n histograms (n x h x w float4, device) rendered at spp
- * against n x h x w RGBA f32 targets (device); *loss = mean squared error of RGB before the step.
- * w must be a multiple of 512 and h of 8. */
-rfk_status rfk_denoiser_train_step(rfk_denoiser* d, const float* bins, uint32_t n, uint32_t w, uint32_t h, double spp,
-                                   const float* targets, float lr, double* loss, void* stream);
+/* One Adam step (learning rate lr) on n histograms (n x h x w float4, device) rendered at spp, with
+ * their tonemapped images (base, n x h x w float4), against n x h x w RGBA f32 targets (device);
+ * *loss = mean squared error of RGB before the step. w must be a multiple of 512 and h of 8. */
+rfk_status rfk_denoiser_train_step(rfk_denoiser* d, const float* bins, const float* base, uint32_t n, uint32_t w,
+                                   uint32_t h, double spp, const float* targets, float lr, double* loss, void* stream);
 /* The loss without a step (validation); w and h multiples of 8. */
-rfk_status rfk_denoiser_loss(rfk_denoiser* d, const float* bins, uint32_t n, uint32_t w, uint32_t h, double spp,
-                             const float* targets, double* loss, void* stream);
+rfk_status rfk_denoiser_loss(rfk_denoiser* d, const float* bins, const float* base, uint32_t n, uint32_t w, uint32_t h,
+                             double spp, const float* targets, double* loss, void* stream);
 /* Parameter gradients of the loss (host array in the parameter layout), without a step. */
-rfk_status rfk_denoiser_gradients(rfk_denoiser* d, const float* bins, uint32_t n, uint32_t w, uint32_t h, double spp,
-                                  const float* targets, float* grads, size_t count, void* stream);
+rfk_status rfk_denoiser_gradients(rfk_denoiser* d, const float* bins, const float* base, uint32_t n, uint32_t w,
+                                  uint32_t h, double spp, const float* targets, float* grads, size_t count, void* stream);
 
-/* denoiser::denoise: the w x h histogram of a render at spp in, the denoised image out in one of
- * RFK_HALF3 / RFK_HALF4 / RFK_FLOAT3 / RFK_FLOAT4 (alpha as the tonemapper's). w and h multiples of 8. */
-rfk_status rfk_denoise(rfk_denoiser* d, const float* bins, uint32_t w, uint32_t h, double spp, void* out, int format,
-                       void* stream);
+/* denoiser::denoise: the w x h histogram of a render at spp and its tonemapped image (base,
+ * float4) in, the denoised image out in one of RFK_HALF3 / RFK_HALF4 / RFK_FLOAT3 / RFK_FLOAT4
+ * (alpha as the tonemapper's). w and h multiples of 8. */
+rfk_status rfk_denoise(rfk_denoiser* d, const float* bins, const float* base, uint32_t w, uint32_t h, double spp,
+                       void* out, int format, void* stream);
 
 #ifdef __cplusplus
 }

@@ -16,7 +16,7 @@ import torch
 F = torch.nn.functional
 
 # (cin, cout, live_in, live_out) as kLayers in denoiser.cpp
-LAYERS = [(32, 32, 6, 32), (32, 32, 32, 32), (32, 64, 32, 64), (64, 64, 64, 64), (64, 128, 64, 128),
+LAYERS = [(32, 32, 9, 32), (32, 32, 32, 32), (32, 64, 32, 64), (64, 64, 64, 64), (64, 128, 64, 128),
           (128, 128, 128, 128), (128, 256, 128, 256), (256, 256, 256, 256), (384, 128, 384, 128),
           (128, 128, 128, 128), (192, 64, 192, 64), (64, 64, 64, 64), (96, 32, 96, 32), (32, 32, 32, 32),
           (32, 32, 32, 3)]
@@ -47,9 +47,10 @@ def _bf16(x: np.ndarray) -> np.ndarray:
     return torch.from_numpy(np.asarray(x, dtype=np.float32)).to(torch.bfloat16).to(torch.float64).numpy()
 
 
-def features(bins: np.ndarray, spp: float, bf16: bool = True) -> np.ndarray:
-    """Input channels of histograms (..., h, w, 4): log1p(density) / 8, mean
-    colour, alpha as the tonemapper's, ln(spp) / 8, zeros to 32 channels."""
+def features(bins: np.ndarray, base: np.ndarray, spp: float, bf16: bool = True) -> np.ndarray:
+    """Input channels of histograms (..., h, w, 4) and their tonemapped images
+    (base, ..., h, w, 4): log1p(density) / 8, mean colour, alpha as the
+    tonemapper's, ln(spp) / 8, base RGB, zeros to 32 channels."""
     b = np.asarray(bins, dtype=np.float64)
     d = b[..., 3]
     f = np.zeros(b.shape[:-1] + (32,))
@@ -60,6 +61,7 @@ def features(bins: np.ndarray, spp: float, bf16: bool = True) -> np.ndarray:
     with np.errstate(divide="ignore"):
         f[..., 4] = np.where(d >= 1, np.clip(np.log(np.maximum(d, 1e-30)) * (4 / np.log(2)) / 96, 0, 1), 0)
     f[..., 5] = np.log(max(spp, 1.0)) / 8
+    f[..., 6:9] = np.asarray(base, dtype=np.float64)[..., :3]
     return _bf16(f) if bf16 else f
 
 
@@ -74,7 +76,8 @@ class _Round(torch.autograd.Function):
 
 
 def forward(x: torch.Tensor, params: list[tuple[torch.Tensor, torch.Tensor]], bf16: bool = True) -> torch.Tensor:
-    """x: (n, 32, h, w); returns the (n, 3, h, w) output (f32 on the GPU)."""
+    """x: (n, 32, h, w); returns the (n, 3, h, w) network output (f32 on the
+    GPU), the correction that is added to the base image."""
     r = _Round.apply if bf16 else (lambda t: t)
 
     def conv(l, t, relu=True):
@@ -119,13 +122,17 @@ def torch_params(flat: np.ndarray, bf16: bool = True, requires_grad: bool = Fals
     return ps
 
 
-def loss_and_gradients(flat: np.ndarray, bins: np.ndarray, spp: float, targets: np.ndarray, bf16: bool = True):
-    """MSE over RGB and its gradients in the flat parameter layout."""
+def _nchw(a: np.ndarray) -> torch.Tensor:
+    return torch.from_numpy(np.asarray(a, dtype=np.float64)[..., :3].transpose(0, 3, 1, 2).copy())
+
+
+def loss_and_gradients(flat: np.ndarray, bins: np.ndarray, base: np.ndarray, spp: float, targets: np.ndarray,
+                       bf16: bool = True):
+    """MSE over RGB of base + output and its gradients in the flat parameter layout."""
     ps = torch_params(flat, bf16=bf16, requires_grad=True)
-    x = torch.from_numpy(features(bins, spp, bf16).transpose(0, 3, 1, 2).copy())
-    t = torch.from_numpy(np.asarray(targets, dtype=np.float64)[..., :3].transpose(0, 3, 1, 2).copy())
-    out = forward(x, ps, bf16=bf16)
-    loss = ((out - t) ** 2).mean()
+    x = torch.from_numpy(features(bins, base, spp, bf16).transpose(0, 3, 1, 2).copy())
+    out = forward(x, ps, bf16=bf16) + _nchw(base)
+    loss = ((out - _nchw(targets)) ** 2).mean()
     loss.backward()
     grads = []
     for w, b in ps:
@@ -134,10 +141,10 @@ def loss_and_gradients(flat: np.ndarray, bins: np.ndarray, spp: float, targets: 
     return float(loss.item()), pack(grads)
 
 
-def denoise(flat: np.ndarray, bins: np.ndarray, spp: float, bf16: bool = True) -> np.ndarray:
-    """Network output clamped to [0, 1], (n, h, w, 3)."""
+def denoise(flat: np.ndarray, bins: np.ndarray, base: np.ndarray, spp: float, bf16: bool = True) -> np.ndarray:
+    """base + network output clamped to [0, 1], (n, h, w, 3)."""
     ps = torch_params(flat, bf16=bf16)
-    x = torch.from_numpy(features(bins, spp, bf16).transpose(0, 3, 1, 2).copy())
+    x = torch.from_numpy(features(bins, base, spp, bf16).transpose(0, 3, 1, 2).copy())
     with torch.no_grad():
-        out = forward(x, ps, bf16=bf16)
+        out = forward(x, ps, bf16=bf16) + _nchw(base)
     return np.clip(out.numpy().transpose(0, 2, 3, 1), 0, 1)

