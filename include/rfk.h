@@ -252,6 +252,21 @@ rfk_status rfk_density_blur(const float* bins_in, float* bins_out, uint32_t w, u
 rfk_status rfk_catmull_coefficients(const double* samples, uint32_t sample_size, uint32_t nseg, float* coeff,
                                     void* stream);
 
+/* ---- output step -----------------------------------------------------------
+ * converter convert_to<In, Out>  assets/kernels/convert.cu:70-99: a half3 /
+ * half4 tonemapped image (RFK_HALF3 / RFK_HALF4) to RFK_FLOAT3 / RFK_FLOAT4 /
+ * RFK_UCHAR3 / RFK_UCHAR4; a byte is min(v * 255, 255) truncated; flip_y
+ * writes rows bottom-up, swap_channels exchanges R and B (BGR output), a
+ * 4-channel output of a 3-channel input gets alpha 1. Device pointers. */
+#define RFK_UCHAR3 4
+#define RFK_UCHAR4 5
+rfk_status rfk_convert(const void* in, int in_format, void* out, int out_format, uint32_t w, uint32_t h, int flip_y,
+                       int swap_channels, void* stream);
+/* Headless artefact (no reference counterpart; the reference encodes frames
+ * with NVENC / nvJPEG): 8-bit RGB or RGBA host pixels, row-major, to a PNG
+ * file. */
+rfk_status rfk_write_png(const char* path, const uint8_t* pixels, uint32_t w, uint32_t h, int channels);
+
 /* fix_rotation  src/librefrakt/src/flame_compiler.cpp:957-1035, host, in place. */
 rfk_status rfk_fix_rotation(double* samples, size_t nsamples, size_t sample_size, size_t flame_size,
                             const size_t* affine_indices, size_t n_affine);

@@ -130,6 +130,9 @@ SIGNATURES = {
     "rfk_batch_image": (C.c_void_p, [C.c_void_p, C.c_size_t]),
     "rfk_batch_params": (C.c_void_p, [C.c_void_p, C.c_size_t]),
     "rfk_batch_get_info": (C.c_int, [C.c_void_p, C.POINTER(BatchInfo)]),
+    "rfk_convert": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_int, C.c_uint32, C.c_uint32, C.c_int, C.c_int,
+                              C.c_void_p]),
+    "rfk_write_png": (C.c_int, [C.c_char_p, C.c_void_p, C.c_uint32, C.c_uint32, C.c_int]),
     # rfk_denoise.h
     "rfk_denoiser_create": (C.c_int, [C.c_uint64, C.POINTER(C.c_void_p)]),
     "rfk_denoiser_destroy": (None, [C.c_void_p]),

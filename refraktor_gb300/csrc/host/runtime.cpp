@@ -765,6 +765,20 @@ rfk_status rfk_tonemap(const float* bins, uint32_t w, uint32_t h, void* out, int
     });
 }
 
+rfk_status rfk_convert(const void* in, int in_format, void* out, int out_format, uint32_t w, uint32_t h, int flip_y,
+                       int swap_channels, void* stream) {
+    return guard([&] {
+        if (!in || !out) fail(RFK_E_INVALID, "null argument");
+        if (in_format != RFK_HALF3 && in_format != RFK_HALF4) fail(RFK_E_INVALID, "input must be RFK_HALF3 or RFK_HALF4");
+        if (out_format != RFK_FLOAT3 && out_format != RFK_FLOAT4 && out_format != RFK_UCHAR3 && out_format != RFK_UCHAR4)
+            fail(RFK_E_INVALID, "output must be RFK_FLOAT3, RFK_FLOAT4, RFK_UCHAR3 or RFK_UCHAR4");
+        if ((uint64_t)w * h > 0xFFFFFFFFull) fail(RFK_E_INVALID, "image too large");
+        cuda_check(rfk_launch_convert(in, in_format == RFK_HALF3 ? 3 : 4, out, out_format, w, h, flip_y, swap_channels,
+                                      (cudaStream_t)stream),
+                   "convert");
+    });
+}
+
 rfk_status rfk_density_histogram(const float* bins, uint32_t count, uint64_t* histogram, uint64_t* max_density,
                                  void* stream) {
     return guard([&] {

@@ -162,6 +162,38 @@ __global__ void red_v4_probe_kernel(float4* __restrict__ buf, unsigned long long
     }
 }
 
+// ---------------------------------------------------------------- convert --
+// convert_to<In, Out> of assets/kernels/convert.cu:70-99: half3 / half4 in,
+// uchar3 / uchar4 / float3 / float4 out; a byte is min(v * 255, 255)
+// truncated (the reference multiplies in double); flip_y writes row h-1-y,
+// swap_channels exchanges R and B; a 4-channel output of a 3-channel input
+// gets alpha 1.
+template <int CIN, int COUT, bool BYTES>
+__global__ void convert_kernel(const __half* __restrict__ in, void* __restrict__ out, unsigned w, unsigned h, int flip_y,
+                               int swap) {
+    const unsigned i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= w * h) return;
+    const __half* p = in + (size_t)i * CIN;
+    float v[4] = {__half2float(p[0]), __half2float(p[1]), __half2float(p[2]), CIN == 4 ? __half2float(p[3]) : 1.0f};
+    if (swap) {
+        const float t = v[0];
+        v[0] = v[2];
+        v[2] = t;
+    }
+    unsigned o = i;
+    if (flip_y) o = (h - i / w - 1) * w + i % w;
+    if (BYTES) {
+        unsigned char* q = static_cast<unsigned char*>(out) + (size_t)o * COUT;
+        for (int c = 0; c < COUT; c++) {
+            const double b = fmin((double)v[c] * 255.0, 255.0);
+            q[c] = (unsigned char)(b > 0.0 ? b : 0.0);
+        }
+    } else {
+        float* q = static_cast<float*>(out) + (size_t)o * COUT;
+        for (int c = 0; c < COUT; c++) q[c] = v[c];
+    }
+}
+
 __global__ void clear_counters_kernel(unsigned long long* c) {
     c[0] = 0;
     c[1] = 0;
@@ -241,6 +273,34 @@ cudaError_t rfk_launch_de_blur(const float4* in, float4* out, unsigned w, unsign
 cudaError_t rfk_launch_red_v4_probe(float4* buf, unsigned long long n, unsigned iters, unsigned blocks, unsigned threads,
                                     cudaStream_t s) {
     red_v4_probe_kernel<<<blocks, threads, 0, s>>>(buf, n, iters, 12345u);
+    return cudaGetLastError();
+}
+
+cudaError_t rfk_launch_convert(const void* in, int in_channels, void* out, int out_format, unsigned w, unsigned h,
+                               int flip_y, int swap, cudaStream_t s) {
+    if (w == 0 || h == 0) return cudaSuccess;
+    const unsigned blocks = (w * h + 255) / 256;
+    const __half* src = static_cast<const __half*>(in);
+    // out_format: 2 float3, 3 float4, 4 uchar3, 5 uchar4
+    if (in_channels == 3) {
+        switch (out_format) {
+        case 2: convert_kernel<3, 3, false><<<blocks, 256, 0, s>>>(src, out, w, h, flip_y, swap); break;
+        case 3: convert_kernel<3, 4, false><<<blocks, 256, 0, s>>>(src, out, w, h, flip_y, swap); break;
+        case 4: convert_kernel<3, 3, true><<<blocks, 256, 0, s>>>(src, out, w, h, flip_y, swap); break;
+        case 5: convert_kernel<3, 4, true><<<blocks, 256, 0, s>>>(src, out, w, h, flip_y, swap); break;
+        default: return cudaErrorInvalidValue;
+        }
+    } else if (in_channels == 4) {
+        switch (out_format) {
+        case 2: convert_kernel<4, 3, false><<<blocks, 256, 0, s>>>(src, out, w, h, flip_y, swap); break;
+        case 3: convert_kernel<4, 4, false><<<blocks, 256, 0, s>>>(src, out, w, h, flip_y, swap); break;
+        case 4: convert_kernel<4, 3, true><<<blocks, 256, 0, s>>>(src, out, w, h, flip_y, swap); break;
+        case 5: convert_kernel<4, 4, true><<<blocks, 256, 0, s>>>(src, out, w, h, flip_y, swap); break;
+        default: return cudaErrorInvalidValue;
+        }
+    } else {
+        return cudaErrorInvalidValue;
+    }
     return cudaGetLastError();
 }
 

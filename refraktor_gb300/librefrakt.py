@@ -459,3 +459,24 @@ class batch:
         i = BatchInfo()
         check(lib().rfk_batch_get_info(self._h, C.byref(i)))
         return {k: getattr(i, k) for k, _ in BatchInfo._fields_}
+
+
+UCHAR3, UCHAR4 = 4, 5
+
+
+class converter:
+    """convert_to<In, Out> (assets/kernels/convert.cu:70-99): a half3 / half4
+    image to float3 / float4 / uchar3 / uchar4, optionally flipped bottom-up
+    and with R and B swapped."""
+
+    def run(self, img, out, dims: Sequence[int], in_fmt: int, out_fmt: int, flip_y: bool = False,
+            swap_channels: bool = False, stream=None) -> None:
+        check(lib().rfk_convert(_dev_ptr(img), in_fmt, _dev_ptr(out), out_fmt, int(dims[0]), int(dims[1]),
+                                1 if flip_y else 0, 1 if swap_channels else 0, _stream_ptr(stream)))
+
+
+def write_png(path: str | Path, pixels: np.ndarray) -> None:
+    """8-bit (h, w, 3 | 4) host pixels to a PNG file."""
+    p = np.ascontiguousarray(pixels, dtype=np.uint8)
+    h, w, c = p.shape
+    check(lib().rfk_write_png(str(path).encode(), p.ctypes.data, w, h, c))

@@ -194,3 +194,34 @@ def test_catmull_matches_reference_kernel():
 def test_red_v4_probe_runs():
     ops = lr.probe_red_v4(4 << 20, 64)
     assert ops > 1e9
+
+
+def _convert_ref(img, cout, as_bytes, flip_y, swap):
+    """numpy restatement of convert_to (assets/kernels/convert.cu:48-99)."""
+    v = img.astype(np.float64)
+    if v.shape[-1] == 3:
+        v = np.concatenate([v, np.ones(v.shape[:-1] + (1,))], -1)
+    if swap:
+        v = v[..., [2, 1, 0, 3]]
+    if flip_y:
+        v = v[::-1]
+    v = v[..., :cout]
+    if as_bytes:
+        return np.maximum(np.minimum(v * 255.0, 255.0), 0).astype(np.uint8)
+    return v.astype(np.float32)
+
+
+@pytest.mark.parametrize("cin", [3, 4])
+@pytest.mark.parametrize("out_fmt", [lr.FLOAT3, lr.FLOAT4, lr.UCHAR3, lr.UCHAR4])
+@pytest.mark.parametrize("flip,swap", [(False, False), (True, True), (True, False)])
+def test_convert_matches_reference_restatement(cin, out_fmt, flip, swap):
+    w, h = 37, 23
+    rng = np.random.default_rng(cin * 10 + out_fmt)
+    img = rng.uniform(-0.05, 1.05, size=(h, w, cin)).astype(np.float16)
+    dev = torch.from_numpy(img).cuda()
+    cout = 3 if out_fmt in (lr.FLOAT3, lr.UCHAR3) else 4
+    as_bytes = out_fmt in (lr.UCHAR3, lr.UCHAR4)
+    out = torch.empty((h, w, cout), dtype=torch.uint8 if as_bytes else torch.float32, device="cuda")
+    lr.converter().run(dev, out, (w, h), lr.HALF3 if cin == 3 else lr.HALF4, out_fmt, flip_y=flip, swap_channels=swap)
+    torch.cuda.synchronize()
+    np.testing.assert_array_equal(out.cpu().numpy(), _convert_ref(img, cout, as_bytes, flip, swap))
