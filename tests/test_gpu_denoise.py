@@ -143,12 +143,12 @@ def test_trained_network_beats_the_plain_low_spp_image():
     from refraktor_gb300 import synthetic as syn
 
     db = lr.flamedb()
-    gs = dn.visible_set(db, syn.hd_flame, list(range(5000, 5000 + 260)), 72, 512, 128)
-    bins, base = dn.render_set(db, gs, 512, 128, 32.0, seed=1, both=True)
-    tgt = dn.render_set(db, gs, 512, 128, 1024.0, seed=2, tonemap=True)
+    gs = dn.visible_set(db, syn.hd_flame, list(range(5000, 5000 + 400)), 72, 512, 256, min_coverage=0.2)
+    bins, base = dn.render_set(db, gs, 512, 256, 32.0, seed=1, both=True)
+    tgt = dn.render_set(db, gs, 512, 256, 1024.0, seed=2, tonemap=True)
     net = dn.denoiser(seed=2)
     dn.train(net, bins[8:], base[8:], tgt[8:], 32.0, steps=200, batch=16)
-    out = torch.empty(128, 512, 4, device="cuda")
+    out = torch.empty(256, 512, 4, device="cuda")
     gains = []
     for i in range(8):
         net.denoise(bins[i], base[i], out, 32.0)
