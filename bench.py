@@ -406,6 +406,48 @@ def run_batch(args) -> dict:
     }
 
 
+DENOISE_WORKLOAD = ("learned denoiser at 1920x1080: 32-spp render + U-Net (trained weights "
+                    "refraktor_gb300/workloads/denoiser_weights.npz) vs the plain path's spp to 40 dB PSNR against an "
+                    "independent 4096-spp render, seeded held-out flames")
+
+
+def run_denoise(args) -> dict:
+    """s/frame to 40 dB PSNR at 1080p: the plain path renders progressively to
+    32..4096 spp and the spp where it crosses 40 dB is interpolated; the
+    denoised path renders 32 spp and runs the U-Net. Both timed on the device."""
+    import torch
+
+    from refraktor_gb300 import build
+    from refraktor_gb300 import denoise as dn
+    from refraktor_gb300 import librefrakt as lr
+    from refraktor_gb300.workloads import train_denoiser as td
+
+    torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+    build.build()
+    db = lr.flamedb()
+    net = dn.denoiser.load(ROOT / "refraktor_gb300" / "workloads" / "denoiser_weights.npz")
+    gs = td.dataset(db, args.flames, td.EVAL_SEED0, 1920, 1080)
+    with ClockSampler(int(os.environ.get("LOCAL_RANK", "0"))) as clocks:
+        ev = td.evaluate(db, net, gs, 1920, 1080)
+    den_s = ev["denoised_s_per_frame"]
+    plain_s = ev["plain_s_per_frame_to_40db_median"]
+    return {
+        "metric": "s/frame to 40 dB PSNR at 1080p (denoised low-spp vs plain)", "value": den_s, "unit": "s/frame",
+        "n_gpus": 1, "steps": len(gs), "warmup": 0, "ms_per_step": 1e3 * den_s, "higher_is_better": False,
+        "scaling": "weak", "vs_baseline": None, "dtype": "bf16", "data": "synthetic (seeded held-out flames)",
+        "config": {"workload": DENOISE_WORKLOAD, "flames": len(gs)},
+        "plain_s_per_frame_to_40db_median": plain_s,
+        "plain_spp_to_40db_median": ev["plain_spp_to_40db_median"],
+        "denoised_psnr_db_mean": ev["psnr_denoised_32spp_mean"],
+        "plain_psnr_db_mean": ev["psnr_plain_mean"],
+        "denoised_reaches_40db": ev["denoised_reaches_40db"],
+        "speedup_where_both_reach_40db_median": ev.get("speedup_where_both_reach_40db_median"),
+        "denoise_ms": ev["denoise_ms"], "plain_ms_per_spp": ev["plain_ms_per_spp"],
+        "e2e": {"value": den_s, "unit": "s/frame", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "clocks": clocks.summary(),
+    }
+
+
 def run_reference(args) -> dict:
     """CPU reference leg: the FP64 oracle port on all host cores."""
     ws, rank = _dist()
@@ -470,14 +512,18 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--workload", default="hd", choices=["hd", "anim", "hetero"],
-                    help="hd: the 1080p single-flame bench (default); anim / hetero: the batched workloads")
+    ap.add_argument("--workload", default="hd", choices=["hd", "anim", "hetero", "denoise"],
+                    help="hd: the 1080p single-flame bench (default); anim / hetero: the batched workloads; "
+                         "denoise: the learned denoiser's s/frame to 40 dB")
+    ap.add_argument("--flames", type=int, default=8, help="evaluation flames of --workload denoise")
     args = ap.parse_args()
     if args.ncu_case:
         run_ncu_case(args)
         return
     if args.impl == "reference":
         line = run_reference(args)
+    elif args.workload == "denoise":
+        line = run_denoise(args)
     elif args.workload != "hd":
         line = run_batch(args)
     else:
