@@ -220,8 +220,8 @@ struct rfk_denoiser {
         const size_t P = (size_t)n * h * w;
         cuda_check(rfk_unet_bias_grad(dy, P, y.d.cout, y.bg, st), "bias grad");
         cuda_check(rfk_unet_to_chw(dy, 1, 1, (int)P, y.d.cout, 0, y.d.cout, 0, s.dyT, st), "transpose");
-        for (int d = 0; d < 3; d++)
-            cuda_check(rfk_unet_to_chw(x, n, h, w, x_cstride, x_coff, y.d.cin, d - 1, s.xT[d], st), "transpose");
+        cuda_check(rfk_unet_to_chw3(x, n, h, w, x_cstride, x_coff, y.d.cin, -1, 3, s.xT[0], s.xT[1], s.xT[2], st),
+                   "transpose");
         const void* xt[3] = {s.xT[0], s.xT[1], s.xT[2]};
         cuda_check(rfk_unet_wgrad3x3(s.dyT, xt, n, h, w, y.d.cout, y.d.cin, y.g, d_err, st), "wgrad");
         if (dx)

@@ -9,23 +9,42 @@ namespace {
 
 using bf16 = __nv_bfloat16;
 
-// 32 pixels x 32 channels through shared memory: reads along channels,
-// writes along x, both coalesced.
-__global__ void to_chw_kernel(const bf16* __restrict__ in, int h, int w, int cstride, int coff, int c, int dx,
-                              bf16* __restrict__ out) {
-    __shared__ bf16 t[32][34];
-    const int xb = blockIdx.x * 32, ny = blockIdx.y, cb = blockIdx.z * 32;
+// Channel-major copies of a channel slice, one per column shift dx in
+// [dx0, dx0 + nshift): a block stages 64 + 2 pixels of one row x 32 channels
+// in shared memory (16-byte loads along channels) and writes each shifted copy
+// with 16-byte stores along x.
+__global__ void to_chw_kernel(const bf16* __restrict__ in, int h, int w, int cstride, int coff, int c, int dx0, int nshift,
+                              bf16* __restrict__ out0, bf16* __restrict__ out1, bf16* __restrict__ out2) {
+    __shared__ __align__(16) bf16 t[66][40];  // [x + 1][channel], rows padded against bank conflicts
+    const int xb = blockIdx.x * 64, ny = blockIdx.y, cb = blockIdx.z * 32;
     const int n = ny / h, y = ny - n * h;
-    for (int i = threadIdx.y; i < 32; i += 8) {
-        const int x = xb + i, sx = x + dx, ch = cb + threadIdx.x;
-        bf16 v = __float2bfloat16(0.0f);
-        if (x < w && sx >= 0 && sx < w && ch < c) v = in[((size_t)ny * w + sx) * cstride + coff + ch];
-        t[i][threadIdx.x] = v;
+    // load: 66 pixels x 4 chunks of 8 channels
+    for (int i = threadIdx.x; i < 66 * 4; i += blockDim.x) {
+        const int px = i >> 2, q = i & 3, x = xb + px - 1, ch = cb + q * 8;
+        uint4 v = make_uint4(0, 0, 0, 0);
+        if (x >= 0 && x < w && ch < c) v = *reinterpret_cast<const uint4*>(in + ((size_t)ny * w + x) * cstride + coff + ch);
+        *reinterpret_cast<uint4*>(&t[px][q * 8]) = v;
     }
     __syncthreads();
-    for (int i = threadIdx.y; i < 32; i += 8) {
-        const int ch = cb + i, x = xb + threadIdx.x;
-        if (ch < c && x < w) out[(((size_t)n * c + ch) * h + y) * w + x] = t[threadIdx.x][i];
+    // store: per shift, 32 channels x 8 chunks of 8 pixels
+    bf16* outs[3] = {out0, out1, out2};
+    for (int sft = 0; sft < nshift; sft++) {
+        const int dx = dx0 + sft;
+        for (int i = threadIdx.x; i < 32 * 8; i += blockDim.x) {
+            const int ch = cb + (i >> 3), x8 = (i & 7) * 8, x = xb + x8;
+            if (ch >= c || x >= w) continue;
+            __align__(16) bf16 v[8];
+#pragma unroll
+            for (int j = 0; j < 8; j++) {
+                const int sx = x + j + dx;
+                v[j] = (sx >= 0 && sx < w) ? t[x8 + j + dx + 1][ch - cb] : __float2bfloat16(0.0f);
+            }
+            bf16* dst = outs[sft] + (((size_t)n * c + ch) * h + y) * w + x;
+            if (x + 8 <= w && (w & 7) == 0)  // rows start 16-byte aligned only when w % 8 == 0
+                *reinterpret_cast<uint4*>(dst) = *reinterpret_cast<uint4*>(v);
+            else
+                for (int j = 0; j < 8 && x + j < w; j++) dst[j] = v[j];
+        }
     }
 }
 
@@ -33,10 +52,19 @@ __global__ void to_chw_kernel(const bf16* __restrict__ in, int h, int w, int cst
 
 extern "C" cudaError_t rfk_unet_to_chw(const void* in, int n_img, int h, int w, int cstride, int coff, int c, int dx,
                                        void* out, cudaStream_t s) {
-    if (n_img <= 0 || h <= 0 || w <= 0 || c <= 0) return cudaErrorInvalidValue;
-    dim3 grid((unsigned)((w + 31) / 32), (unsigned)(n_img * h), (unsigned)((c + 31) / 32));
-    to_chw_kernel<<<grid, dim3(32, 8), 0, s>>>(static_cast<const bf16*>(in), h, w, cstride, coff, c, dx,
-                                               static_cast<bf16*>(out));
+    return rfk_unet_to_chw3(in, n_img, h, w, cstride, coff, c, dx, 1, out, nullptr, nullptr, s);
+}
+
+extern "C" cudaError_t rfk_unet_to_chw3(const void* in, int n_img, int h, int w, int cstride, int coff, int c, int dx0,
+                                        int nshift, void* out0, void* out1, void* out2, cudaStream_t s) {
+    if (n_img <= 0 || h <= 0 || w <= 0 || c <= 0 || c % 8 || cstride % 8 || coff % 8 || nshift < 1 || nshift > 3)
+        return cudaErrorInvalidValue;
+    const void* ptrs[4] = {in, out0, out1, out2};
+    for (const void* p : ptrs)
+        if (reinterpret_cast<size_t>(p) & 15) return cudaErrorMisalignedAddress;
+    dim3 grid((unsigned)((w + 63) / 64), (unsigned)(n_img * h), (unsigned)((c + 31) / 32));
+    to_chw_kernel<<<grid, 256, 0, s>>>(static_cast<const bf16*>(in), h, w, cstride, coff, c, dx0, nshift,
+                                       static_cast<bf16*>(out0), static_cast<bf16*>(out1), static_cast<bf16*>(out2));
     return cudaGetLastError();
 }
 
@@ -79,55 +107,98 @@ __global__ void features_kernel(const float4* __restrict__ bins, const float4* _
     for (int q = 0; q < 4; q++) o[q] = reinterpret_cast<uint4*>(h)[q];
 }
 
+// The layers below move 8 channels (16 bytes) per thread; channel counts,
+// strides and offsets are multiples of 8 (32 in this network).
+__device__ __forceinline__ void ld8(const bf16* p, float (&v)[8]) {
+    const uint4 u = *reinterpret_cast<const uint4*>(p);
+    const __nv_bfloat162* h = reinterpret_cast<const __nv_bfloat162*>(&u);
+#pragma unroll
+    for (int j = 0; j < 4; j++) {
+        const float2 f = __bfloat1622float2(h[j]);
+        v[2 * j] = f.x;
+        v[2 * j + 1] = f.y;
+    }
+}
+
+__device__ __forceinline__ void st8(bf16* p, const float (&v)[8]) {
+    __nv_bfloat162 h[4];
+#pragma unroll
+    for (int j = 0; j < 4; j++) h[j] = __floats2bfloat162_rn(v[2 * j], v[2 * j + 1]);
+    *reinterpret_cast<uint4*>(p) = *reinterpret_cast<uint4*>(h);
+}
+
 // 2x2 average pool of a channel slice: out[n][y][x][c] = mean of in[n][2y..2y+1][2x..2x+1][coff + c].
 __global__ void avgpool_kernel(const bf16* __restrict__ in, int h, int w, int cstride, int coff, int c,
-                               bf16* __restrict__ out, size_t total) {
-    const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+                               bf16* __restrict__ out, unsigned total) {
+    const unsigned i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= total) return;
-    const int ch = (int)(i % c);
-    size_t r = i / c;
-    const int ho = h / 2, wo = w / 2;
+    const int c8 = c / 8, ho = h / 2, wo = w / 2;
+    const int q = (int)(i % c8);
+    unsigned r = i / c8;
     const int x = (int)(r % wo);
     r /= wo;
     const int y = (int)(r % ho);
-    const size_t n = r / ho;
-    const size_t b = ((n * h + 2 * y) * w + 2 * x) * cstride + coff + ch;
-    const float s = bf(in[b]) + bf(in[b + cstride]) + bf(in[b + (size_t)w * cstride]) + bf(in[b + (size_t)w * cstride + cstride]);
-    out[i] = __float2bfloat16(0.25f * s);
+    const unsigned n = r / ho;
+    const size_t b = (((size_t)n * h + 2 * y) * w + 2 * x) * cstride + coff + q * 8;
+    float a[8], v[8];
+    ld8(in + b, a);
+    ld8(in + b + cstride, v);
+#pragma unroll
+    for (int j = 0; j < 8; j++) a[j] += v[j];
+    ld8(in + b + (size_t)w * cstride, v);
+#pragma unroll
+    for (int j = 0; j < 8; j++) a[j] += v[j];
+    ld8(in + b + (size_t)w * cstride + cstride, v);
+#pragma unroll
+    for (int j = 0; j < 8; j++) a[j] = 0.25f * (a[j] + v[j]);
+    st8(out + (size_t)i * 8, a);
 }
 
 // Nearest 2x upsample into a channel slice: out[n][y][x][coff + c] = in[n][y / 2][x / 2][c].
 __global__ void upsample_kernel(const bf16* __restrict__ in, int h, int w, int c, bf16* __restrict__ out, int cstride,
-                                int coff, size_t total) {
-    const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+                                int coff, unsigned total) {
+    const unsigned i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= total) return;
-    const int ch = (int)(i % c);
-    size_t r = i / c;
-    const int W = 2 * w, H = 2 * h;
+    const int c8 = c / 8, W = 2 * w, H = 2 * h;
+    const int q = (int)(i % c8);
+    unsigned r = i / c8;
     const int x = (int)(r % W);
     r /= W;
     const int y = (int)(r % H);
-    const size_t n = r / H;
-    out[((n * H + y) * W + x) * cstride + coff + ch] = in[((n * h + y / 2) * w + x / 2) * c + ch];
+    const unsigned n = r / H;
+    const uint4 v = *reinterpret_cast<const uint4*>(in + (((size_t)n * h + y / 2) * w + x / 2) * c + q * 8);
+    *reinterpret_cast<uint4*>(out + (((size_t)n * H + y) * W + x) * cstride + coff + q * 8) = v;
 }
 
 // Gradient through a nearest 2x upsample (sum of the 2x2 block of a channel
 // slice of g), times the ReLU derivative of the upsampled activation:
 // out[n][y][x][c] = (act > 0) * sum g[n][2y..][2x..][gcoff + c].
 __global__ void up_backward_kernel(const bf16* __restrict__ g, int gcstride, int gcoff, const bf16* __restrict__ act,
-                                   int h, int w, int c, bf16* __restrict__ out, size_t total) {
-    const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+                                   int h, int w, int c, bf16* __restrict__ out, unsigned total) {
+    const unsigned i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= total) return;
-    const int ch = (int)(i % c);
-    size_t r = i / c;
+    const int c8 = c / 8;
+    const int q = (int)(i % c8);
+    unsigned r = i / c8;
     const int x = (int)(r % w);
     r /= w;
     const int y = (int)(r % h);
-    const size_t n = r / h;
+    const unsigned n = r / h;
     const int W = 2 * w;
-    const size_t b = ((n * 2 * h + 2 * y) * W + 2 * x) * gcstride + gcoff + ch;
-    const float s = bf(g[b]) + bf(g[b + gcstride]) + bf(g[b + (size_t)W * gcstride]) + bf(g[b + (size_t)W * gcstride + gcstride]);
-    out[i] = __float2bfloat16(bf(act[i]) > 0.0f ? s : 0.0f);
+    const size_t b = (((size_t)n * 2 * h + 2 * y) * W + 2 * x) * gcstride + gcoff + q * 8;
+    float a[8], v[8], m[8];
+    ld8(g + b, a);
+    ld8(g + b + gcstride, v);
+#pragma unroll
+    for (int j = 0; j < 8; j++) a[j] += v[j];
+    ld8(g + b + (size_t)W * gcstride, v);
+#pragma unroll
+    for (int j = 0; j < 8; j++) a[j] += v[j];
+    ld8(g + b + (size_t)W * gcstride + gcstride, v);
+    ld8(act + (size_t)i * 8, m);
+#pragma unroll
+    for (int j = 0; j < 8; j++) a[j] = m[j] > 0.0f ? a[j] + v[j] : 0.0f;
+    st8(out + (size_t)i * 8, a);
 }
 
 // Gradient of a skip activation s (a channel slice of a concatenation) that
@@ -135,20 +206,24 @@ __global__ void up_backward_kernel(const bf16* __restrict__ g, int gcstride, int
 // derivative: out = (s > 0) * (gcat[slice] + gpool[y / 2][x / 2] / 4).
 __global__ void skip_backward_kernel(const bf16* __restrict__ gcat, int cstride, int coff, const bf16* __restrict__ gpool,
                                      const bf16* __restrict__ cat, int h, int w, int c, bf16* __restrict__ out,
-                                     size_t total) {
-    const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+                                     unsigned total) {
+    const unsigned i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= total) return;
-    const int ch = (int)(i % c);
-    size_t r = i / c;
+    const int c8 = c / 8;
+    const int q = (int)(i % c8);
+    unsigned r = i / c8;
     const int x = (int)(r % w);
     r /= w;
     const int y = (int)(r % h);
-    const size_t n = r / h;
-    const size_t px = (n * h + y) * w + x;
-    const float s = bf(cat[px * cstride + coff + ch]);
-    const float gp = bf(gpool[((n * (h / 2) + y / 2) * (w / 2) + x / 2) * c + ch]);
-    const float v = bf(gcat[px * cstride + coff + ch]) + 0.25f * gp;
-    out[i] = __float2bfloat16(s > 0.0f ? v : 0.0f);
+    const unsigned n = r / h;
+    const size_t px = ((size_t)n * h + y) * w + x;
+    float sv[8], gc[8], gp[8];
+    ld8(cat + px * cstride + coff + q * 8, sv);
+    ld8(gcat + px * cstride + coff + q * 8, gc);
+    ld8(gpool + (((size_t)n * (h / 2) + y / 2) * (w / 2) + x / 2) * c + q * 8, gp);
+#pragma unroll
+    for (int j = 0; j < 8; j++) gc[j] = sv[j] > 0.0f ? gc[j] + 0.25f * gp[j] : 0.0f;
+    st8(out + (size_t)i * 8, gc);
 }
 
 // Mean squared error of the prediction base + out[0..2] (out f32, cstride 32;
@@ -177,21 +252,30 @@ __global__ void mse_kernel(const float* __restrict__ out, const float4* __restri
     if ((threadIdx.x & 31) == 0 && l != 0.0f) atomicAdd(loss, (double)l);
 }
 
-// Per-channel sum over pixels (bias gradient): db[c] += sum_p g[p][c].
-__global__ void bias_grad_kernel(const bf16* __restrict__ g, size_t npx, int c, float* __restrict__ db) {
-    // block: 256 threads = 8 pixel lanes x 32 channels (a channel group of 32)
-    const int cg = blockIdx.y * 32 + (threadIdx.x & 31);
-    const int lanep = threadIdx.x >> 5;
-    float s = 0.0f;
-    for (size_t p = (size_t)blockIdx.x * 8 + lanep; p < npx; p += (size_t)gridDim.x * 8) s += bf(g[p * c + cg]);
-    __shared__ float red[8][32];
-    red[lanep][threadIdx.x & 31] = s;
+// Per-channel sum over pixels (bias gradient): db[c] += sum_p g[p][c]. A
+// thread sums one 8-channel chunk over a strided run of pixels; the block
+// reduces in shared memory and adds once per channel.
+__global__ void bias_grad_kernel(const bf16* __restrict__ g, unsigned npx, int c, float* __restrict__ db) {
+    extern __shared__ float red[];  // [c]
+    const int c8 = c / 8;
+    for (int j = threadIdx.x; j < c; j += blockDim.x) red[j] = 0.0f;
     __syncthreads();
-    if (threadIdx.x < 32) {
-        float t = 0.0f;
-        for (int k = 0; k < 8; k++) t += red[k][threadIdx.x];
-        atomicAdd(db + blockIdx.y * 32 + threadIdx.x, t);
+    const int q = threadIdx.x % c8;
+    const int lanes = blockDim.x / c8;
+    const int lane = threadIdx.x / c8;
+    float acc[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+    if (lane < lanes) {
+        for (unsigned p = blockIdx.x * lanes + lane; p < npx; p += gridDim.x * lanes) {
+            float v[8];
+            ld8(g + (size_t)p * c + q * 8, v);
+#pragma unroll
+            for (int j = 0; j < 8; j++) acc[j] += v[j];
+        }
+#pragma unroll
+        for (int j = 0; j < 8; j++) atomicAdd(&red[q * 8 + j], acc[j]);
     }
+    __syncthreads();
+    for (int j = threadIdx.x; j < c; j += blockDim.x) atomicAdd(db + j, red[j]);
 }
 
 // Adam (Kingma & Ba 2015) on one conv layer's f32 master weights [cout][9][cin]
@@ -276,39 +360,40 @@ extern "C" cudaError_t rfk_unet_features(const float4* bins, const float4* base,
 
 extern "C" cudaError_t rfk_unet_avgpool(const void* in, int n_img, int h, int w, int cstride, int coff, int c, void* out,
                                         cudaStream_t s) {
-    const size_t total = (size_t)n_img * (h / 2) * (w / 2) * c;
-    if (h % 2 || w % 2 || total == 0) return cudaErrorInvalidValue;
+    const size_t total = (size_t)n_img * (h / 2) * (w / 2) * (c / 8);
+    if (h % 2 || w % 2 || total == 0 || c % 8 || cstride % 8 || coff % 8 || total > 0xFFFFFFFFull) return cudaErrorInvalidValue;
     avgpool_kernel<<<blocks_for(total), 256, 0, s>>>(static_cast<const bf16*>(in), h, w, cstride, coff, c,
-                                                      static_cast<bf16*>(out), total);
+                                                      static_cast<bf16*>(out), (unsigned)total);
     return cudaGetLastError();
 }
 
 extern "C" cudaError_t rfk_unet_upsample(const void* in, int n_img, int h, int w, int c, void* out, int cstride, int coff,
                                          cudaStream_t s) {
-    const size_t total = (size_t)n_img * 4 * h * w * c;
-    if (total == 0) return cudaErrorInvalidValue;
+    const size_t total = (size_t)n_img * 4 * h * w * (c / 8);
+    if (total == 0 || c % 8 || cstride % 8 || coff % 8 || total > 0xFFFFFFFFull) return cudaErrorInvalidValue;
     upsample_kernel<<<blocks_for(total), 256, 0, s>>>(static_cast<const bf16*>(in), h, w, c, static_cast<bf16*>(out),
-                                                       cstride, coff, total);
+                                                       cstride, coff, (unsigned)total);
     return cudaGetLastError();
 }
 
 extern "C" cudaError_t rfk_unet_up_backward(const void* g, int gcstride, int gcoff, const void* act, int n_img, int h, int w,
                                             int c, void* out, cudaStream_t s) {
-    const size_t total = (size_t)n_img * h * w * c;
-    if (total == 0) return cudaErrorInvalidValue;
+    const size_t total = (size_t)n_img * h * w * (c / 8);
+    if (total == 0 || c % 8 || gcstride % 8 || gcoff % 8 || total > 0xFFFFFFFFull) return cudaErrorInvalidValue;
     up_backward_kernel<<<blocks_for(total), 256, 0, s>>>(static_cast<const bf16*>(g), gcstride, gcoff,
                                                           static_cast<const bf16*>(act), h, w, c, static_cast<bf16*>(out),
-                                                          total);
+                                                          (unsigned)total);
     return cudaGetLastError();
 }
 
 extern "C" cudaError_t rfk_unet_skip_backward(const void* gcat, int cstride, int coff, const void* gpool, const void* cat,
                                               int n_img, int h, int w, int c, void* out, cudaStream_t s) {
-    const size_t total = (size_t)n_img * h * w * c;
-    if (total == 0 || h % 2 || w % 2) return cudaErrorInvalidValue;
+    const size_t total = (size_t)n_img * h * w * (c / 8);
+    if (total == 0 || h % 2 || w % 2 || c % 8 || cstride % 8 || coff % 8 || total > 0xFFFFFFFFull)
+        return cudaErrorInvalidValue;
     skip_backward_kernel<<<blocks_for(total), 256, 0, s>>>(static_cast<const bf16*>(gcat), cstride, coff,
                                                             static_cast<const bf16*>(gpool), static_cast<const bf16*>(cat),
-                                                            h, w, c, static_cast<bf16*>(out), total);
+                                                            h, w, c, static_cast<bf16*>(out), (unsigned)total);
     return cudaGetLastError();
 }
 
@@ -321,10 +406,12 @@ extern "C" cudaError_t rfk_unet_mse(const float* out, const float4* base, const 
 }
 
 extern "C" cudaError_t rfk_unet_bias_grad(const void* g, size_t npx, int c, float* db, cudaStream_t s) {
-    if (c % 32 || npx == 0) return cudaErrorInvalidValue;
-    unsigned bx = (unsigned)((npx + 8 * 256 - 1) / (8 * 256));
-    if (bx > 1024) bx = 1024;
-    bias_grad_kernel<<<dim3(bx, (unsigned)(c / 32)), 256, 0, s>>>(static_cast<const bf16*>(g), npx, c, db);
+    if (c % 8 || c > 2048 || npx == 0 || npx > 0xFFFFFFFFull) return cudaErrorInvalidValue;
+    const unsigned lanes = 256 / (c / 8) > 0 ? 256 / (c / 8) : 1;
+    unsigned bx = (unsigned)((npx + lanes * 64 - 1) / (lanes * 64));
+    if (bx > 152 * 4) bx = 152 * 4;
+    const unsigned threads = (c / 8) > 256 ? (unsigned)(c / 8) : 256;
+    bias_grad_kernel<<<bx, threads, (size_t)c * sizeof(float), s>>>(static_cast<const bf16*>(g), (unsigned)npx, c, db);
     return cudaGetLastError();
 }
 

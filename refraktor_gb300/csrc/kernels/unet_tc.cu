@@ -30,6 +30,7 @@
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <mutex>
 
 #include "tc_ptx.cuh"
@@ -57,12 +58,17 @@ struct conv_args {
 
 template <int BK, int BN>
 struct conv_cfg {
-    static constexpr uint32_t A_BYTES = 128u * BK * 2u;
+    // R image rows per tile (R accumulators of 128 x BN): small-N layers move
+    // R times the bytes per pipeline stage, so the stage round trip is shared
+    static constexpr int R = BN >= 128 ? 1 : 128 / BN;
+    static constexpr uint32_t A_ROW = 128u * BK * 2u;  // one image row segment
+    static constexpr uint32_t A_BYTES = R * A_ROW;
     static constexpr uint32_t B_BYTES = (uint32_t)BN * BK * 2u;
     static constexpr uint32_t STAGE_BYTES = A_BYTES + B_BYTES;
-    // BN 256: one CTA per SM, 4 stages; otherwise about 96 KB for two CTAs per SM
-    static constexpr int STAGES = BN == 256 ? 4 : (98304u / STAGE_BYTES > 8 ? 8 : (int)(98304u / STAGE_BYTES));
+    // one persistent CTA per SM: as many stages as fit in ~190 KB, at most 8
+    static constexpr int STAGES = (194560u / STAGE_BYTES > 8) ? 8 : (int)(194560u / STAGE_BYTES);
     static constexpr uint32_t SMEM = STAGES * STAGE_BYTES + 1024u;
+    static constexpr uint32_t TMEM_COLS = 2u * R * BN;  // two sets of R accumulators
 };
 
 __device__ __forceinline__ void store_bf16x32(bf16* dst, const float (&v)[32]) {
@@ -91,33 +97,71 @@ __device__ __forceinline__ void load_bf16x32(const bf16* src, float (&v)[32]) {
     }
 }
 
+__device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(tc::smem_u32(bar)) : "memory");
+}
+
+__device__ __forceinline__ void store_bf16x16(bf16* dst, const float (&v)[16]) {
+    uint4* d = reinterpret_cast<uint4*>(dst);
+#pragma unroll
+    for (int q = 0; q < 2; q++) {
+        __nv_bfloat162 h[4];
+#pragma unroll
+        for (int j = 0; j < 4; j++) h[j] = __floats2bfloat162_rn(v[8 * q + 2 * j], v[8 * q + 2 * j + 1]);
+        d[q] = *reinterpret_cast<uint4*>(h);
+    }
+}
+
+__device__ __forceinline__ void load_bf16x16(const bf16* src, float (&v)[16]) {
+    const uint4* s = reinterpret_cast<const uint4*>(src);
+#pragma unroll
+    for (int q = 0; q < 2; q++) {
+        uint4 u = s[q];
+        const __nv_bfloat162* h = reinterpret_cast<const __nv_bfloat162*>(&u);
+#pragma unroll
+        for (int j = 0; j < 4; j++) {
+            float2 f = __bfloat1622float2(h[j]);
+            v[8 * q + 2 * j] = f.x;
+            v[8 * q + 2 * j + 1] = f.y;
+        }
+    }
+}
+
+constexpr int kEpiWarps = 8;  // two warps per TMEM lane quarter, each half of the columns
+
+// Persistent: one CTA per SM walks the tiles (R rows x 128-pixel segment x BN
+// output channels) t = blockIdx.x, blockIdx.x + gridDim.x, ...
+// Warps 0-7: epilogue (warp w reads TMEM lane quarter w % 4, column half
+// w / 4), warp 8 lane 0: TMA producer over a ring of stages that runs across
+// tiles, warp 9 lane 0: MMA issuer. Two TMEM accumulators: the MMAs of tile
+// i + 1 run while the epilogue drains tile i (acc_full / acc_empty barriers).
 template <int BK, int BN>
-__global__ void __launch_bounds__(128) conv3x3_tc(const __grid_constant__ CUtensorMap tmA,
-                                                  const __grid_constant__ CUtensorMap tmB, conv_args p) {
+__global__ void __launch_bounds__(320, 1) conv3x3_tc(const __grid_constant__ CUtensorMap tmA,
+                                                     const __grid_constant__ CUtensorMap tmB, conv_args p) {
     using C = conv_cfg<BK, BN>;
     extern __shared__ uint8_t smem_dyn[];
     uint8_t* base = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_dyn) + 1023) & ~(uintptr_t)1023);
-    __shared__ uint64_t full[C::STAGES], empty[C::STAGES], done;
+    __shared__ uint64_t full[C::STAGES], empty[C::STAGES], acc_full[2], acc_empty[2];
     __shared__ uint32_t tmem_base;
     __shared__ int s_fail;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
 
-    const int mt = blockIdx.x;
-    const int xt = mt % p.tiles_x;
-    const int y = (mt / p.tiles_x) % p.h;
-    const int img = mt / (p.tiles_x * p.h);
-    const int x0 = xt * 128;
-    const int n0 = blockIdx.y * BN;
-    const int kpt = p.cin / BK;  // K blocks per tap
+    const int ntn = p.cout / BN;                           // N tiles
+    const int rows_t = (p.h + C::R - 1) / C::R;            // row groups per image
+    const int ntiles = p.n_img * rows_t * p.tiles_x * ntn;
+    const int kpt = p.cin / BK;                            // K blocks per tap
     const int nk = 9 * kpt;
 
-    if (warp == 0) tc::tmem_alloc(&tmem_base, BN);
+    if (warp == 0) tc::tmem_alloc(&tmem_base, C::TMEM_COLS);
     if (threadIdx.x == 32) {
         for (int s = 0; s < C::STAGES; s++) {
             tc::mbar_init(&full[s], 1);
             tc::mbar_init(&empty[s], 1);
         }
-        tc::mbar_init(&done, 1);
+        for (int b = 0; b < 2; b++) {
+            tc::mbar_init(&acc_full[b], 1);
+            tc::mbar_init(&acc_empty[b], kEpiWarps);  // one arrival per epilogue warp
+        }
         s_fail = 0;
         tc::mbar_fence_init();
     }
@@ -126,107 +170,151 @@ __global__ void __launch_bounds__(128) conv3x3_tc(const __grid_constant__ CUtens
     tc::fence_after();
     const uint32_t tmem = tmem_base;
 
-    if (warp == 0 && lane == 0) {
-        // producer: TMA loads into the stage ring
-        int issued = 0;
-        bool ok = true;
-        for (int kb = 0; kb < nk; kb++) {
-            const int s = kb % C::STAGES, r = kb / C::STAGES;
-            if (r > 0 && !tc::mbar_wait(&empty[s], (r - 1) & 1)) {
-                ok = false;
-                break;
+    if (warp == kEpiWarps) {
+        if (lane == 0) {
+            // producer: the stage ring runs across tiles
+            uint32_t g = 0;
+            bool ok = true;
+            for (int t = blockIdx.x; ok && t < ntiles; t += gridDim.x) {
+                const int mt = t / ntn, n0 = (t - mt * ntn) * BN;
+                const int xt = mt % p.tiles_x;
+                const int y = ((mt / p.tiles_x) % rows_t) * C::R;
+                const int img = mt / (p.tiles_x * rows_t);
+                for (int kb = 0; kb < nk; kb++, g++) {
+                    const uint32_t s = g % C::STAGES, r = g / C::STAGES;
+                    if (r > 0 && !tc::mbar_wait(&empty[s], (r - 1) & 1)) {
+                        ok = false;
+                        break;
+                    }
+                    const int tap = kb / kpt, cb = kb - tap * kpt;
+                    uint8_t* sa = base + (size_t)s * C::STAGE_BYTES;
+                    tc::mbar_expect_tx(&full[s], C::STAGE_BYTES);
+                    tc::tma_load_4d(sa, &tmA, &full[s], p.cin_off + cb * BK, xt * 128 + tap % 3 - 1, y + tap / 3 - 1, img);
+                    tc::tma_load_2d(sa + C::A_BYTES, &tmB, &full[s], tap * p.cin + cb * BK, n0);
+                }
             }
-            const int tap = kb / kpt, cb = kb - tap * kpt;
-            const int dy = tap / 3 - 1, dx = tap % 3 - 1;
-            uint8_t* sa = base + (size_t)s * C::STAGE_BYTES;
-            tc::mbar_expect_tx(&full[s], C::STAGE_BYTES);
-            tc::tma_load_4d(sa, &tmA, &full[s], p.cin_off + cb * BK, x0 + dx, y + dy, img);
-            tc::tma_load_2d(sa + C::A_BYTES, &tmB, &full[s], tap * p.cin + cb * BK, n0);
-            issued++;
+            if (!ok) {
+                atomicExch(&s_fail, 1);
+                // let the copies in flight land before the CTA exits (bounded)
+                for (uint32_t q = g >= (uint32_t)C::STAGES ? g - C::STAGES : 0; q < g; q++)
+                    tc::mbar_wait(&full[q % C::STAGES], (q / C::STAGES) & 1);
+            }
         }
-        if (!ok) {
-            atomicExch(&s_fail, 1);
-            // let the copies in flight land before the CTA exits (bounded)
-            for (int kb = issued - C::STAGES < 0 ? 0 : issued - C::STAGES; kb < issued; kb++)
-                tc::mbar_wait(&full[kb % C::STAGES], (kb / C::STAGES) & 1);
+    } else if (warp == kEpiWarps + 1) {
+        if (lane == 0) {
+            constexpr uint32_t idesc = tc::idesc_bf16(128, BN);
+            uint32_t g = 0;
+            bool ok = true;
+            int i = 0;
+            for (int t = blockIdx.x; ok && t < ntiles; t += gridDim.x, i++) {
+                const int b = i & 1;
+                if (i >= 2 && !tc::mbar_wait(&acc_empty[b], ((i >> 1) - 1) & 1)) {
+                    ok = false;
+                    break;
+                }
+                tc::fence_after();
+                const uint32_t acc = tmem + (uint32_t)(b * C::R * BN);
+                for (int kb = 0; kb < nk; kb++, g++) {
+                    const uint32_t s = g % C::STAGES;
+                    if (!tc::mbar_wait(&full[s], (g / C::STAGES) & 1)) {
+                        ok = false;
+                        break;
+                    }
+                    tc::fence_after();
+                    const uint32_t sa = tc::smem_u32(base + (size_t)s * C::STAGE_BYTES), sb = sa + C::A_BYTES;
+#pragma unroll
+                    for (int r = 0; r < C::R; r++)
+#pragma unroll
+                        for (int kk = 0; kk < BK / 16; kk++)
+                            tc::mma_bf16(acc + (uint32_t)(r * BN), tc::smem_desc(sa + r * C::A_ROW + kk * 32, BK * 2),
+                                         tc::smem_desc(sb + kk * 32, BK * 2), idesc, (kb | kk) != 0 ? 1u : 0u);
+                    tc::mma_commit(&empty[s]);
+                }
+                tc::mma_commit(&acc_full[b]);  // also on failure: arrives once the issued MMAs are done
+            }
+            if (!ok) atomicExch(&s_fail, 1);
         }
-    } else if (warp == 1 && lane == 0) {
-        // MMA issuer
-        constexpr uint32_t idesc = tc::idesc_bf16(128, BN);
-        bool ok = true;
-        for (int kb = 0; kb < nk; kb++) {
-            const int s = kb % C::STAGES, r = kb / C::STAGES;
-            if (!tc::mbar_wait(&full[s], r & 1)) {
-                ok = false;
+    } else {
+        // epilogue: warps 0-7; TMEM lane 32 * (warp % 4) + lane = tile row,
+        // columns [half * BN / 2, (half + 1) * BN / 2)
+        const int quarter = warp & 3, half = warp >> 2;
+        int i = 0;
+        for (int t = blockIdx.x; t < ntiles; t += gridDim.x, i++) {
+            const int b = i & 1;
+            bool got = tc::mbar_wait(&acc_full[b], (i >> 1) & 1);
+            got = __all_sync(0xffffffffu, got);
+            if (!got) {
+                if (lane == 0) atomicExch(&s_fail, 1);
                 break;
             }
             tc::fence_after();
-            const uint32_t sa = tc::smem_u32(base + (size_t)s * C::STAGE_BYTES), sb = sa + C::A_BYTES;
-#pragma unroll
-            for (int kk = 0; kk < BK / 16; kk++)
-                tc::mma_bf16(tmem, tc::smem_desc(sa + kk * 32, BK * 2), tc::smem_desc(sb + kk * 32, BK * 2), idesc,
-                             (kb | kk) != 0 ? 1u : 0u);
-            tc::mma_commit(&empty[s]);
-        }
-        tc::mma_commit(&done);
-        if (!ok) atomicExch(&s_fail, 1);
-    }
-    __syncwarp();
-
-    // epilogue: TMEM lane 32 * warp + lane = tile row
-    bool got = tc::mbar_wait(&done, 0);
-    got = __all_sync(0xffffffffu, got);
-    tc::fence_after();
-    if (got) {
-        const int row = warp * 32 + lane;
-        const int x = x0 + row;
-        const bool valid = x < p.w;
-        const size_t pix = ((size_t)img * p.h + y) * p.w + (valid ? x : 0);
+            const int mt = t / ntn, n0 = (t - mt * ntn) * BN;
+            const int xt = mt % p.tiles_x;
+            const int y0 = ((mt / p.tiles_x) % rows_t) * C::R;
+            const int img = mt / (p.tiles_x * rows_t);
+            const int x = xt * 128 + quarter * 32 + lane;
 #pragma unroll 1
-        for (int c = 0; c < BN; c += 32) {
-            float v[32];
-            tc::tmem_ld32(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)c, v);
-            const int ch = n0 + c;
-            if (valid && ch < p.cout) {
-                if (p.bias) {
+            for (int r = 0; r < C::R; r++) {
+                const int y = y0 + r;
+                const bool valid = x < p.w && y < p.h;
+                const size_t pix = ((size_t)img * p.h + (valid ? y : 0)) * p.w + (valid ? x : 0);
+#pragma unroll 1
+                for (int c = half * (BN / 2); c < (half + 1) * (BN / 2); c += 16) {
+                    float v[16];
+                    tc::tmem_ld16(tmem + ((uint32_t)(quarter * 32) << 16) + (uint32_t)((b * C::R + r) * BN + c), v);
+                    const int ch = n0 + c;
+                    if (!valid) continue;
+                    if (p.bias) {
+                        const float4* bb = reinterpret_cast<const float4*>(p.bias + ch);
 #pragma unroll
-                    for (int j = 0; j < 32; j++) v[j] += p.bias[ch + j];
-                }
-                if (p.relu) {
-#pragma unroll
-                    for (int j = 0; j < 32; j++) v[j] = fmaxf(v[j], 0.0f);
-                }
-                if (p.mask) {
-                    float m[32];
-                    load_bf16x32(p.mask + pix * p.mask_cstride + p.mask_coff + ch, m);
-#pragma unroll
-                    for (int j = 0; j < 32; j++) v[j] = m[j] > 0.0f ? v[j] : 0.0f;
-                }
-                const size_t at = pix * p.out_cstride + p.out_coff + ch;
-                if (p.out_f32) {
-                    float4* dst = reinterpret_cast<float4*>(static_cast<float*>(p.out) + at);
-#pragma unroll
-                    for (int q = 0; q < 8; q++) {
-                        float4 o = p.accumulate ? dst[q] : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-                        dst[q] = make_float4(v[4 * q] + o.x, v[4 * q + 1] + o.y, v[4 * q + 2] + o.z, v[4 * q + 3] + o.w);
+                        for (int q = 0; q < 4; q++) {
+                            const float4 f = __ldg(bb + q);
+                            v[4 * q] += f.x;
+                            v[4 * q + 1] += f.y;
+                            v[4 * q + 2] += f.z;
+                            v[4 * q + 3] += f.w;
+                        }
                     }
-                } else {
-                    bf16* dst = static_cast<bf16*>(p.out) + at;
-                    if (p.accumulate) {
-                        float o[32];
-                        load_bf16x32(dst, o);
+                    if (p.relu) {
 #pragma unroll
-                        for (int j = 0; j < 32; j++) v[j] += o[j];
+                        for (int j = 0; j < 16; j++) v[j] = fmaxf(v[j], 0.0f);
                     }
-                    store_bf16x32(dst, v);
+                    if (p.mask) {
+                        float m[16];
+                        load_bf16x16(p.mask + pix * p.mask_cstride + p.mask_coff + ch, m);
+#pragma unroll
+                        for (int j = 0; j < 16; j++) v[j] = m[j] > 0.0f ? v[j] : 0.0f;
+                    }
+                    const size_t at = pix * p.out_cstride + p.out_coff + ch;
+                    if (p.out_f32) {
+                        float4* dst = reinterpret_cast<float4*>(static_cast<float*>(p.out) + at);
+#pragma unroll
+                        for (int q = 0; q < 4; q++) {
+                            float4 o = p.accumulate ? dst[q] : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+                            dst[q] = make_float4(v[4 * q] + o.x, v[4 * q + 1] + o.y, v[4 * q + 2] + o.z, v[4 * q + 3] + o.w);
+                        }
+                    } else {
+                        bf16* dst = static_cast<bf16*>(p.out) + at;
+                        if (p.accumulate) {
+                            float o[16];
+                            load_bf16x16(dst, o);
+#pragma unroll
+                            for (int j = 0; j < 16; j++) v[j] += o[j];
+                        }
+                        store_bf16x16(dst, v);
+                    }
                 }
             }
+            // the accumulator may be overwritten once all epilogue warps have read it
+            tc::fence_before();
+            __syncwarp();
+            if (lane == 0) mbar_arrive(&acc_empty[b]);
         }
     }
     tc::fence_before();
     __syncthreads();
-    if (threadIdx.x == 0 && (!got || s_fail)) atomicExch(p.err, 1);
-    if (warp == 0) tc::tmem_dealloc(tmem, BN);
+    if (threadIdx.x == 0 && s_fail) atomicExch(p.err, 1);
+    if (warp == 0) tc::tmem_dealloc(tmem, C::TMEM_COLS);
 }
 
 // ----------------------------------------------------------------- wgrad ----
@@ -389,6 +477,17 @@ cudaError_t raise_smem(K kernel, uint32_t bytes) {
     return cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
 }
 
+int sm_count_cached() {
+    static int n = 0;
+    if (!n) {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
+        if (n <= 0) n = 1;
+    }
+    return n;
+}
+
 template <int BK, int BN>
 cudaError_t launch_conv(const CUtensorMap& a, const CUtensorMap& b, const conv_args& p, cudaStream_t s) {
     using C = conv_cfg<BK, BN>;
@@ -396,8 +495,10 @@ cudaError_t launch_conv(const CUtensorMap& a, const CUtensorMap& b, const conv_a
     static cudaError_t attr = cudaSuccess;
     std::call_once(once, [] { attr = raise_smem(conv3x3_tc<BK, BN>, C::SMEM); });
     if (attr != cudaSuccess) return attr;
-    dim3 grid((unsigned)(p.n_img * p.h * p.tiles_x), (unsigned)(p.cout / BN));
-    conv3x3_tc<BK, BN><<<grid, 128, C::SMEM, s>>>(a, b, p);
+    const long long tiles = (long long)p.n_img * ((p.h + C::R - 1) / C::R) * p.tiles_x * (p.cout / BN);
+    if (tiles > 0x7FFFFFFFLL) return cudaErrorInvalidValue;
+    const int grid = (int)std::min<long long>(tiles, sm_count_cached());
+    conv3x3_tc<BK, BN><<<grid, 32 * (kEpiWarps + 2), C::SMEM, s>>>(a, b, p);
     return cudaGetLastError();
 }
 
@@ -439,7 +540,9 @@ extern "C" cudaError_t rfk_unet_conv3x3(const void* in, int n_img, int h, int w,
     {
         cuuint64_t dims[4] = {(cuuint64_t)in_cstride, (cuuint64_t)w, (cuuint64_t)h, (cuuint64_t)n_img};
         cuuint64_t str[3] = {(cuuint64_t)in_cstride * 2, (cuuint64_t)w * in_cstride * 2, (cuuint64_t)h * w * in_cstride * 2};
-        cuuint32_t box[4] = {(cuuint32_t)bk, 128, 1, 1};
+        // R image rows per tile, as conv_cfg<BK, BN>::R
+        const cuuint32_t rows = bn >= 128 ? 1u : (cuuint32_t)(128 / bn);
+        cuuint32_t box[4] = {(cuuint32_t)bk, 128, rows, 1};
         if (!make_map(&ma, in, 4, dims, str, box, sw)) return cudaErrorInvalidValue;
     }
     {

@@ -218,3 +218,49 @@ def train(net: denoiser, bins, base, targets, spp: float, steps: int, batch: int
         vl = float(np.mean([net.loss(vb[i:i + 4].contiguous(), vbase[i:i + 4].contiguous(), spp, vt[i:i + 4].contiguous())
                             for i in range(0, vb.shape[0], 4)]))
     return train_report(steps, dt, losses[0], float(np.mean(losses[-20:])), vl, 1e3 * dt / max(steps, 1))
+
+
+def _profile_case(argv=None) -> None:
+    """Fixed workloads for timing and profiler captures, with random inputs:
+    `infer` runs the U-Net on a 1920 x 1080 histogram, `train` runs training
+    steps on 16 x 512 x 512."""
+    import argparse
+
+    import torch
+
+    from . import build
+
+    ap = argparse.ArgumentParser(prog="python -m refraktor_gb300.denoise")
+    ap.add_argument("--case", choices=["infer", "train"], default="infer")
+    ap.add_argument("--reps", type=int, default=3)
+    a = ap.parse_args(argv)
+    build.build()
+    net = denoiser.load(Path(__file__).resolve().parent / "workloads" / "denoiser_weights.npz")
+    g = torch.Generator(device="cuda").manual_seed(1)
+    if a.case == "infer":
+        bins = torch.rand(1080, 1920, 4, device="cuda", generator=g) * 8
+        base = torch.rand(1080, 1920, 4, device="cuda", generator=g)
+        out = torch.empty(1080, 1920, 4, device="cuda")
+        for _ in range(a.reps):
+            net.denoise(bins, base, out, 32.0)
+    else:
+        bins = torch.rand(16, 512, 512, 4, device="cuda", generator=g) * 8
+        base = torch.rand(16, 512, 512, 4, device="cuda", generator=g)
+        tgt = torch.rand(16, 512, 512, 4, device="cuda", generator=g)
+        for _ in range(a.reps):
+            net.train_step(bins, base, 32.0, tgt, 1e-4)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(a.reps):
+        if a.case == "infer":
+            net.denoise(bins, base, out, 32.0)
+        else:
+            net.train_step(bins, base, 32.0, tgt, 1e-4)
+    e1.record()
+    torch.cuda.synchronize()
+    print(f"{a.case}: {e0.elapsed_time(e1) / a.reps:.3f} ms per call")
+
+
+if __name__ == "__main__":
+    _profile_case()
