@@ -132,7 +132,10 @@ rfk_status rfk_kernel_source(const rfk_kernel* k, char* buf, size_t cap, size_t*
  * output, nsamples >= 4); the spline segments between samples 1 and
  * nsamples-2 are spread over the persistent blocks as temporal samples. The
  * state owns a cleared w x h float4 histogram (device), chain states and
- * counters. temporal_multiplier must be 1. */
+ * counters. temporal_multiplier T (1..32): T x grid temporal samples, each with
+ * its own chains; a persistent block cycles through its T samples during bin
+ * (motion blur over the segment with T times the samples at the same chain
+ * count), each (block, sample) reaching an equal share of the quality. */
 rfk_status rfk_warmup(const rfk_kernel* k, const double* samples, size_t nsamples, uint32_t w, uint32_t h,
                       uint32_t seed, uint32_t warmup_count, int temporal_multiplier, void* stream, rfk_state** out);
 void rfk_state_destroy(rfk_state* s);
@@ -142,6 +145,8 @@ typedef struct {
     uint32_t iters;   /* passes per chain cap for this call (0 = none) */
     uint32_t millis;  /* time budget; 0 or above 60000 means 60000 (every call ends) */
     double quality;   /* additional spp to reach (0 = none) */
+    uint32_t temporal_slicing; /* passes a block spends on one temporal sample before the next
+                                  (temporal_multiplier > 1); 0 = 100, as flame_kernel::bin */
 } rfk_bailout;
 
 /* flame_kernel::bin_result  flame_compiler.h:27-35 (+ status bits and draw count) */

@@ -26,7 +26,7 @@ class KernelInfo(C.Structure):
 
 
 class Bailout(C.Structure):
-    _fields_ = [("iters", C.c_uint32), ("millis", C.c_uint32), ("quality", C.c_double)]
+    _fields_ = [("iters", C.c_uint32), ("millis", C.c_uint32), ("quality", C.c_double), ("temporal_slicing", C.c_uint32)]
 
 
 class BinResult(C.Structure):

@@ -59,8 +59,11 @@ struct dev_bin_args {
     unsigned long long time_ns;
     const volatile unsigned* stop;
     unsigned long long* counters;
+    unsigned tmul;
+    unsigned slice;
 };
-constexpr int kCounterWords = 6;  // quality, passes, start, stop, draws, status|pad
+constexpr int kCounterWords = 6;
+constexpr int kMaxTemporalMultiplier = 32;  // RFK_MAX_TMUL of rfk_iterate.cuh  // quality, passes, start, stop, draws, status|pad
 constexpr uint32_t kMaxBinMillis = 60000;  // upper bound of one bin call
 
 }  // namespace
@@ -69,6 +72,7 @@ struct rfk_state {
     std::shared_ptr<const kernel_impl> k;
     unsigned w = 0, h = 0, seed = 0;
     int grid = 0;
+    int tmul = 1;  // temporal samples per persistent block
     size_t nchains = 0;
     float* d_samples = nullptr;
     float *d_x = nullptr, *d_y = nullptr, *d_c = nullptr;
@@ -197,6 +201,7 @@ std::shared_ptr<kernel_impl> compile(const rfk::flamedb& db, const rfk::flame& f
     cuda_check(cudaLibraryGetKernel(&k->f_bin, k->lib, "rfk_bin"), "rfk_bin");
     cuda_check(cudaLibraryGetKernel(&k->f_apply, k->lib, "rfk_apply"), "rfk_apply");
     cuda_check(cudaLibraryGetKernel(&k->f_bin_batch, k->lib, "rfk_bin_batch"), "rfk_bin_batch");
+    cuda_check(cudaLibraryGetKernel(&k->f_bin_tm, k->lib, "rfk_bin_tm"), "rfk_bin_tm");
     cudaFuncAttributes fa{};
     cuda_check(cudaFuncGetAttributes(&fa, reinterpret_cast<const void*>(k->f_bin)), "attributes");
     k->regs = fa.numRegs;
@@ -498,7 +503,8 @@ rfk_status rfk_warmup(const rfk_kernel* kh, const double* samples, size_t nsampl
         if (!samples || !out) fail(RFK_E_INVALID, "null argument");
         if (w == 0 || h == 0) fail(RFK_E_INVALID, "image size must be positive");
         if ((uint64_t)w * h > (1ull << 31)) fail(RFK_E_INVALID, "image too large");
-        if (temporal_multiplier != 1) fail(RFK_E_INVALID, "temporal_multiplier must be 1");
+        if (temporal_multiplier < 1 || temporal_multiplier > kMaxTemporalMultiplier)
+            fail(RFK_E_INVALID, "temporal_multiplier must be in [1, 32]");
         cudaStream_t s = (cudaStream_t)stream;
         auto st = std::make_unique<rfk_state>();
         st->k = k;
@@ -506,11 +512,14 @@ rfk_status rfk_warmup(const rfk_kernel* kh, const double* samples, size_t nsampl
         st->h = h;
         st->seed = seed;
         st->grid = k->grid;
-        st->nchains = (size_t)k->grid * k->block * k->cpt;
+        st->tmul = temporal_multiplier;
+        // T x grid temporal samples, each with its own parameter block and chains
+        const unsigned nsmp = (unsigned)st->grid * (unsigned)temporal_multiplier;
+        st->nchains = (size_t)nsmp * k->block * k->cpt;
         std::vector<unsigned> seg;
         std::vector<float> t;
-        temporal_schedule((unsigned)st->grid, (unsigned)(nsamples - 3), seg, t);
-        cuda_check(cudaMalloc(&st->d_samples, (size_t)st->grid * k->sample_floats * sizeof(float)), "alloc samples");
+        temporal_schedule(nsmp, (unsigned)(nsamples - 3), seg, t);
+        cuda_check(cudaMalloc(&st->d_samples, (size_t)nsmp * k->sample_floats * sizeof(float)), "alloc samples");
         prepare(*k, samples, nsamples, seg, t, seed, st->d_samples, s);
         cuda_check(cudaMalloc(&st->d_x, st->nchains * sizeof(float)), "alloc chains");
         cuda_check(cudaMalloc(&st->d_y, st->nchains * sizeof(float)), "alloc chains");
@@ -529,7 +538,7 @@ rfk_status rfk_warmup(const rfk_kernel* kh, const double* samples, size_t nsampl
         dev_chains ch{st->d_x, st->d_y, st->d_c, st->d_last};
         unsigned ww = w, hh = h, sd = seed, salt = k->salt, wc = warmup_count;
         void* args[] = {&st->d_samples, &ch, &ww, &hh, &sd, &salt, &wc};
-        launch(k->f_warmup, (unsigned)st->grid, (unsigned)k->block, s, args, "rfk_warmup");
+        launch(k->f_warmup, nsmp, (unsigned)k->block, s, args, "rfk_warmup");
         cuda_check(cudaStreamSynchronize(s), "warmup");
         *out = st.release();
     });
@@ -573,8 +582,13 @@ rfk_status rfk_bin_async(rfk_state* st, const rfk_bailout* bo, void* stream) {
         a.time_ns = (unsigned long long)ms * 1000000ull;
         a.stop = st->d_stop;
         a.counters = st->d_counters;
+        a.tmul = (unsigned)st->tmul;
+        a.slice = bo->temporal_slicing ? bo->temporal_slicing : 100u;
         void* args[] = {&a};
-        launch(k.f_bin, (unsigned)st->grid, (unsigned)k.block, s, args, "rfk_bin");
+        if (st->tmul > 1)
+            launch(k.f_bin_tm, (unsigned)st->grid, (unsigned)k.block, s, args, "rfk_bin_tm");
+        else
+            launch(k.f_bin, (unsigned)st->grid, (unsigned)k.block, s, args, "rfk_bin");
         cuda_check(rfk_launch_density_histogram(st->d_bins, st->w * st->h, st->d_counters + kCounterWords,
                                                 st->d_counters + kCounterWords + 97, s),
                    "density histogram");
@@ -642,7 +656,7 @@ rfk_status rfk_state_chains(rfk_state* st, float* x, float* y, float* c, size_t 
 rfk_status rfk_state_samples(rfk_state* st, float* out, size_t cap, size_t* count) {
     return guard([&] {
         if (!st) fail(RFK_E_INVALID, "null state");
-        const size_t n = (size_t)st->grid * st->k->sample_floats;
+        const size_t n = (size_t)st->grid * st->tmul * st->k->sample_floats;
         if (count) *count = n;
         if (!out) return;
         if (cap < n) fail(RFK_E_INVALID, "output buffer too small");

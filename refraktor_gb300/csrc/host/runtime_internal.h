@@ -96,7 +96,8 @@ struct kernel_impl {
     std::string source;
     std::string log;
     cudaLibrary_t lib = nullptr;
-    cudaKernel_t f_prepare = nullptr, f_warmup = nullptr, f_bin = nullptr, f_apply = nullptr, f_bin_batch = nullptr;
+    cudaKernel_t f_prepare = nullptr, f_warmup = nullptr, f_bin = nullptr, f_apply = nullptr, f_bin_batch = nullptr,
+                 f_bin_tm = nullptr;
     int block = 256, cpt = 1, flush = 0, sort = 0, grid = 0, regs = 0;
     size_t sample_floats = 0;
     double compile_ms = 0.0;

@@ -508,6 +508,8 @@ struct rfk_bin_args {
     unsigned long long time_ns;         // time budget per block (0 = none)
     const volatile unsigned* stop;      // host-written stop flag (may be null)
     rfk_counters* counters;
+    unsigned tmul;                      // temporal samples per block (rfk_bin_tm)
+    unsigned slice;                     // passes per temporal sample before switching (rfk_bin_tm)
 };
 
 // Rotates the per-lane chain slots by one (slot q takes slot q + 1), with
@@ -799,6 +801,155 @@ extern "C" __global__ void RFK_BIN_BOUNDS rfk_warmup(const float* __restrict__ s
 #if RFK_CHAOS
         st.last[chain[k]] = (unsigned char)last[k];
 #endif
+    }
+}
+
+// ------------------------------------------------- temporal multiplier ----
+// flame_kernel::bin with temporal_multiplier T > 1 (refactor.cu:404-475,
+// flamelib.h:203-260): the state holds T x grid temporal samples, each with
+// its own parameter block and chains; block b owns samples b + grid * i
+// (i < T) and cycles through them, `slice` passes at a time, saving and
+// loading the chains in global memory. Each (block, sample) pair stops at an
+// equal share of the quality target, so every temporal sample contributes
+// alike (the motion-blur average); the block ends when all its samples are
+// done or on the pass cap, time budget or stop flag.
+#define RFK_MAX_TMUL 32
+extern "C" __global__ void RFK_BIN_BOUNDS rfk_bin_tm(rfk_bin_args a) {
+    __shared__ __align__(16) float P[RFK_SAMPLE_FLOATS];
+    __shared__ unsigned long long s_hits, s_draws, s_start;
+    __shared__ unsigned long long s_q[RFK_MAX_TMUL];
+    __shared__ unsigned s_bail, s_done;
+    __shared__ int s_next;
+    __shared__ rfk_pass_smem sm;
+    rfk_pass_smem_init(sm);
+    const unsigned T = a.tmul;
+    const unsigned S = gridDim.x * T;
+    const unsigned lane_stream = blockIdx.x * RFK_BLOCK + threadIdx.x;
+    const unsigned long long share = a.quality_target ? (a.quality_target + S - 1) / S : 0ull;
+    if (threadIdx.x == 0) {
+        s_hits = 0;
+        s_draws = 0;
+        s_bail = 0;
+        s_done = 0;
+        s_start = rfk_time();
+        atomicMin(&a.counters->start_ns, s_start);
+    }
+    for (unsigned i = threadIdx.x; i < RFK_MAX_TMUL; i += RFK_BLOCK) s_q[i] = 0;
+    float x[RFK_CPT], y[RFK_CPT], c[RFK_CPT];
+    unsigned last[RFK_CPT], chain[RFK_CPT];
+    int cur = 0;
+    unsigned smp = blockIdx.x;
+    for (unsigned i = threadIdx.x; i < RFK_SAMPLE_FLOATS; i += RFK_BLOCK) P[i] = a.samples[(size_t)smp * RFK_SAMPLE_FLOATS + i];
+#pragma unroll
+    for (int k = 0; k < RFK_CPT; k++) {
+        chain[k] = (k * S + smp) * RFK_BLOCK + threadIdx.x;
+        x[k] = a.st.x[chain[k]];
+        y[k] = a.st.y[chain[k]];
+        c[k] = a.st.c[chain[k]];
+#if RFK_CHAOS
+        last[k] = a.st.last[chain[k]];
+#else
+        last[k] = 255u;
+#endif
+    }
+    __syncthreads();
+
+    unsigned long long pass = 0, total = 0;
+    unsigned in_slice = 0;
+    unsigned my_hits = 0, my_draws = 0;
+#pragma unroll 1
+    for (;;) {
+        unsigned n = 0;
+#pragma unroll 1
+        for (; n < a.check && (a.max_passes == 0 || total < a.max_passes); n++) {
+            int kk[RFK_CPT];
+            rfk_pick_sort(x, y, c, last, kk, sm, P, lane_stream, a.call_id, pass, a.seed, a.salt);
+#pragma unroll 1
+            for (int k = 0; k < RFK_CPT; k++)
+                rfk_move_slot(x, y, c, kk, last, chain, sm, P, a.bins, a.w, a.h, a.call_id, pass, a.seed, a.salt, true,
+                              my_hits, my_draws);
+            pass++;
+            total++;
+        }
+        in_slice += n;
+        rfk_block_totals(my_hits, my_draws, &s_hits, &s_draws, sm, a.bins);
+        if (threadIdx.x == 0) {
+            atomicAdd(&a.counters->quality, s_hits);
+            atomicAdd(&a.counters->draws, s_draws);
+            s_q[cur] += s_hits;
+            s_hits = 0;
+            s_draws = 0;
+            unsigned done = s_done;
+            if (share && s_q[cur] >= share) done |= 1u << cur;
+            s_done = done;
+            unsigned bail = 0;
+            if (done == (T >= 32 ? 0xFFFFFFFFu : ((1u << T) - 1u))) bail |= RFK_ST_QUALITY;
+            if (a.max_passes && total >= a.max_passes) bail |= RFK_ST_ITERS;
+            if (a.time_ns && rfk_time() - s_start >= a.time_ns) bail |= RFK_ST_TIME;
+            if (a.stop && *a.stop) bail |= RFK_ST_STOP;
+            s_bail = bail;
+            int nxt = cur;
+            if (!bail && ((done >> cur) & 1u || in_slice >= a.slice)) {
+                // next sample not yet done, round robin
+                for (unsigned j = 1; j <= T; j++) {
+                    const int cand = (int)((cur + j) % T);
+                    if (!((done >> cand) & 1u)) {
+                        nxt = cand;
+                        break;
+                    }
+                }
+            }
+            s_next = nxt;
+        }
+        __syncthreads();
+        if (s_bail) break;
+        const int nxt = s_next;
+        if (nxt != cur) {
+            // park this sample's chains, bring in the next sample
+#pragma unroll
+            for (int k = 0; k < RFK_CPT; k++) {
+                a.st.x[chain[k]] = x[k];
+                a.st.y[chain[k]] = y[k];
+                a.st.c[chain[k]] = c[k];
+#if RFK_CHAOS
+                a.st.last[chain[k]] = (unsigned char)last[k];
+#endif
+            }
+            cur = nxt;
+            smp = blockIdx.x + gridDim.x * (unsigned)cur;
+            for (unsigned i = threadIdx.x; i < RFK_SAMPLE_FLOATS; i += RFK_BLOCK)
+                P[i] = a.samples[(size_t)smp * RFK_SAMPLE_FLOATS + i];
+#pragma unroll
+            for (int k = 0; k < RFK_CPT; k++) {
+                chain[k] = (k * S + smp) * RFK_BLOCK + threadIdx.x;
+                x[k] = a.st.x[chain[k]];
+                y[k] = a.st.y[chain[k]];
+                c[k] = a.st.c[chain[k]];
+#if RFK_CHAOS
+                last[k] = a.st.last[chain[k]];
+#else
+                last[k] = 255u;
+#endif
+            }
+            in_slice = 0;
+            __syncthreads();
+        } else if (in_slice >= a.slice) {
+            in_slice = 0;
+        }
+    }
+#pragma unroll
+    for (int k = 0; k < RFK_CPT; k++) {
+        a.st.x[chain[k]] = x[k];
+        a.st.y[chain[k]] = y[k];
+        a.st.c[chain[k]] = c[k];
+#if RFK_CHAOS
+        a.st.last[chain[k]] = (unsigned char)last[k];
+#endif
+    }
+    if (threadIdx.x == 0) {
+        atomicAdd(&a.counters->passes, total * (unsigned long long)(RFK_BLOCK * RFK_CPT));
+        atomicOr(&a.counters->status, s_bail);
+        atomicMax(&a.counters->stop_ns, rfk_time());
     }
 }
 

@@ -152,10 +152,12 @@ class flame:
 
 @dataclass
 class bailout_args:
-    """flame_compiler.h:92-96 (iters is a per-chain pass cap here)."""
+    """flame_compiler.h:92-96 (iters is a per-chain pass cap here), plus the
+    temporal slicing of flame_kernel::bin (0 = 100 passes)."""
     iters: int = 0
     millis: int = 1000
     quality: float = 128.0
+    temporal_slicing: int = 0
 
 
 @dataclass
@@ -218,13 +220,13 @@ class flame_kernel:
 
     def bin(self, state: "saved_state", bo: bailout_args, stream=None) -> bin_result:
         """flame_kernel::bin(stream, state, bailout) (waits for the result)."""
-        b = Bailout(bo.iters, bo.millis, bo.quality)
+        b = Bailout(bo.iters, bo.millis, bo.quality, bo.temporal_slicing)
         r = BinResult()
         check(lib().rfk_bin(state._h, C.byref(b), _stream_ptr(stream), C.byref(r)))
         return bin_result(**r.as_dict())
 
     def bin_async(self, state: "saved_state", bo: bailout_args, stream=None) -> None:
-        b = Bailout(bo.iters, bo.millis, bo.quality)
+        b = Bailout(bo.iters, bo.millis, bo.quality, bo.temporal_slicing)
         check(lib().rfk_bin_async(state._h, C.byref(b), _stream_ptr(stream)))
 
     def apply_xform(self, params: np.ndarray, xform: int, points: np.ndarray, seed: int = 0) -> np.ndarray:

@@ -329,3 +329,65 @@ def test_sort_and_flush_variants_agree(db, comp, sort, flush):
     o2, _ = orc.render(g, w, h, chains_k, passes, seed=2, threads=8, params=p_ref, palette=pal, hammersley=True)
     floor = np.abs(o1[..., 3] / o1[..., 3].sum() - o2[..., 3] / o2[..., 3].sum()).sum()
     assert np.abs(a - c).sum() < 1.25 * floor + 0.002, (np.abs(a - c).sum(), floor)
+
+
+def _schedule(S, nseg):
+    """temporal_schedule of runtime.cpp (refactor.cu:266-270)."""
+    size = S // nseg
+    seg, t = [], []
+    for s in range(S):
+        sg, tt = s // size, (s % size) / float(S // nseg)
+        if sg >= nseg:
+            sg, tt = nseg - 1, 1.0
+        seg.append(sg)
+        t.append(tt)
+    return seg, t
+
+
+def test_temporal_multiplier_static_flame_matches_single_sample_render(db, comp):
+    """temporal_multiplier T > 1 (flame_kernel::warmup / bin with T x grid
+    temporal samples cycled by the persistent blocks): on a static genome the
+    render matches the T = 1 render within the noise floor of two T = 1 seeds,
+    the quality target is met (an equal share per block and sample), and the
+    state holds T x grid prepared samples."""
+    g = syn.hd_flame(2)
+    f = lr.flame.from_json(db, g)
+    k = comp.get_flame_kernel(db, f)
+    w, h = 160, 120
+    samples = f.pack_samples(4, w, h)
+
+    def render(T, seed):
+        st = k.warmup(samples, (w, h), seed=seed, count=20, temporal_multiplier=T)
+        r = k.bin(st, lr.bailout_args(iters=0, millis=0, quality=96.0, temporal_slicing=8))
+        assert r.status & 1, r
+        assert 96.0 <= r.quality <= 96.0 * 1.3, r.quality
+        d = st.bins().cpu().numpy().astype(np.float64)[..., 3]
+        return st, d / d.sum()
+
+    st4, d4 = render(4, 5)
+    assert st4.samples().shape[0] == 4 * k.info["grid"]
+    _, d1 = render(1, 5)
+    _, d1b = render(1, 6)
+    assert np.abs(d4 - d1).sum() < 1.3 * np.abs(d1 - d1b).sum()
+
+
+def test_temporal_multiplier_spreads_samples_over_the_segment(db, comp):
+    """With T x grid temporal samples the prepared parameter blocks follow the
+    reference schedule over the spline segments, T times finer: each equals
+    rfk_prepare_samples at the same (segment, t) up to the screen jitter."""
+    keys = lr.align_flames(db, [lr.flame.from_json(db, syn.hd_flame(40 + i, n_xforms=4, final=False)) for i in range(4)])
+    k = comp.get_flame_kernel(db, keys[0])
+    w, h = 96, 64
+    samples = np.stack([f.pack_sample(w, h) for f in keys])
+    T = 3
+    st = k.warmup(samples, (w, h), seed=9, count=4, temporal_multiplier=T)
+    got = st.samples().astype(np.float64)
+    S = T * k.info["grid"]
+    seg, t = _schedule(S, samples.shape[0] - 3)
+    want = k.prepare_samples(samples, seg, t, seed=9).astype(np.float64)
+    assert got.shape == want.shape
+    pal0 = k.info["sample_floats"] - 1024
+    idx = np.r_[0:4, 6:pal0]
+    ulp = np.spacing(np.maximum(np.abs(got), np.abs(want)).astype(np.float32)).astype(np.float64)
+    assert np.all(np.abs(got - want)[:, idx] <= 4 * ulp[:, idx])
+    assert np.all(np.abs(got - want)[:, pal0:] <= 1.0 / 255 + 1e-6)
