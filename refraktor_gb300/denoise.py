@@ -192,9 +192,9 @@ class train_report:
 
 
 def train(net: denoiser, bins, base, targets, spp: float, steps: int, batch: int = 16, lr_: float = 1e-3,
-          val: Optional[tuple] = None, seed: int = 0, log=None) -> train_report:
-    """Adam on random mini-batches of the (N, h, w, 4) training tensors;
-    cosine-decayed learning rate. val: (bins, base, targets)."""
+          val: Optional[tuple] = None, seed: int = 0, log=None, augment: bool = True) -> train_report:
+    """Adam on random mini-batches of the (N, h, w, 4) training tensors,
+    randomly mirrored; cosine-decayed learning rate. val: (bins, base, targets)."""
     import torch
 
     g = torch.Generator(device="cpu").manual_seed(seed)
@@ -205,8 +205,13 @@ def train(net: denoiser, bins, base, targets, spp: float, steps: int, batch: int
     for s in range(steps):
         idx = torch.randint(0, n, (batch,), generator=g).cuda()
         lr_s = lr_ * 0.5 * (1.0 + np.cos(np.pi * s / max(steps, 1)))
-        l = net.train_step(bins.index_select(0, idx).contiguous(), base.index_select(0, idx).contiguous(), spp,
-                           targets.index_select(0, idx).contiguous(), max(lr_s, lr_ * 0.02))
+        b, bb, tt = bins.index_select(0, idx), base.index_select(0, idx), targets.index_select(0, idx)
+        if augment:
+            # mirror images: the chaos game's statistics do not depend on orientation
+            flips = [d for d, bit in ((1, 1), (2, 2)) if int(torch.randint(0, 4, (1,), generator=g)) & bit]
+            if flips:
+                b, bb, tt = b.flip(flips), bb.flip(flips), tt.flip(flips)
+        l = net.train_step(b.contiguous(), bb.contiguous(), spp, tt.contiguous(), max(lr_s, lr_ * 0.02))
         losses.append(l)
         if log and (s % 100 == 0 or s == steps - 1):
             log(f"step {s} loss {l:.6f}")

@@ -6,7 +6,7 @@ against the plain path (the learned-denoiser workload):
                each from the 14-variation set), visibility-rejected and framed
                at 512 x 512; input: the 32-spp histogram and its tonemapped
                image, target: the tonemapped 4096-spp render; Adam, lr 1e-3
-               (cosine decay), batch 16
+               (cosine decay), batch 16, random mirroring
   evaluation   `--eval` held-out seeded flames at 1920 x 1080: the plain path
                renders to 32, 64, ..., 4096 spp (one progressive render), the
                denoised path denoises its 32-spp histogram; both are scored by

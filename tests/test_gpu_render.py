@@ -353,14 +353,16 @@ def test_temporal_multiplier_static_flame_matches_single_sample_render(db, comp)
     g = syn.hd_flame(2)
     f = lr.flame.from_json(db, g)
     k = comp.get_flame_kernel(db, f)
-    w, h = 160, 120
+    # each (block, sample) share must span several check intervals of 1024
+    # chains, or the first check already overshoots it (as in the reference)
+    w, h = 320, 240
     samples = f.pack_samples(4, w, h)
 
     def render(T, seed):
         st = k.warmup(samples, (w, h), seed=seed, count=20, temporal_multiplier=T)
-        r = k.bin(st, lr.bailout_args(iters=0, millis=0, quality=96.0, temporal_slicing=8))
+        r = k.bin(st, lr.bailout_args(iters=0, millis=0, quality=256.0, temporal_slicing=8))
         assert r.status & 1, r
-        assert 96.0 <= r.quality <= 96.0 * 1.3, r.quality
+        assert 256.0 <= r.quality <= 256.0 * 1.3, r.quality
         d = st.bins().cpu().numpy().astype(np.float64)[..., 3]
         return st, d / d.sum()
 
