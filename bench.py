@@ -478,7 +478,7 @@ def run_ncu_case(args) -> None:
     """Small case for ncu captures of rfk_bin: the 1080p workload genome,
     warm-up, then `--ncu-launches` bin launches to `--ncu-spp` spp each
     (16 spp: ~0.5 ms; 1024 spp is the bench step), with
-    the autotuned options unless --flush/--cpt/--block/--sort are given."""
+    the autotuned options unless --flush/--cpt/--block/--sort/--minb are given."""
     from refraktor_gb300 import build
     from refraktor_gb300 import librefrakt as lr
 
@@ -489,7 +489,8 @@ def run_ncu_case(args) -> None:
     if args.flush is None:
         opts, _ = lr.autotune(db, f, samples, (W, H))
     else:
-        opts = dict(flush=args.flush, chains_per_thread=args.cpt, block=args.block, sort=args.sort)
+        opts = dict(flush=args.flush, chains_per_thread=args.cpt, block=args.block, sort=args.sort,
+                    blocks_per_sm=args.minb)
     k = lr.flame_compiler().get_flame_kernel(db, f, **opts)
     st = k.warmup(samples, (W, H), 1, WARMUP_PASSES)
     for _ in range(args.ncu_launches):
@@ -506,6 +507,7 @@ def main():
     ap.add_argument("--cpt", type=int, default=4)
     ap.add_argument("--block", type=int, default=256)
     ap.add_argument("--sort", type=int, default=2)
+    ap.add_argument("--minb", type=int, default=0, help="blocks_per_sm of the --ncu-case kernel (0 = library default)")
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)

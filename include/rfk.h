@@ -88,9 +88,10 @@ typedef struct {
     int flush;             /* histogram update: 0 = red.global.add.v4.f32 per draw, 1 = warp-aggregated,
                               2 = warp-aggregated into a per-block shared-memory cache of hot pixels,
                               3 = the shared-memory cache without warp aggregation */
-    int blocks_per_sm;     /* 0 = as many as fit; n > 0 = at most n bin blocks per SM, and
-                              registers capped so that n fit (launch bounds) */
-    int sort;              /* 0 or 1 = sort each warp's chains by xform every pass, 2 = sort the whole
+    int blocks_per_sm;     /* 0 = registers capped so that 1280 / block bin blocks fit per SM, and as
+                              many run as fit; n > 0 = registers capped so that n fit, and at most n
+                              run per SM (launch bounds) */
+    int sort;              /* 1 = sort each warp's chains by xform every pass, 0 or 2 = sort the whole
                               block's chains (both when 2..32 xforms); -1 = never */
 } rfk_compile_opts;
 

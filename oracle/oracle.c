@@ -322,22 +322,25 @@ typedef struct {
     int hammersley;
     double* hist;
     uint64_t draws;
-    double wsum;
-    double cum[MAX_XF];
+    /* pick weights: row 0 the xform weights, row 1 + r (chaos) the chaos row
+       of previous xform r times the xform weights (flame.tpl:170-177) */
+    double wt[MAX_XF + 1][MAX_XF];
+    double wsum[MAX_XF + 1];
+    double cum[MAX_XF + 1][MAX_XF];
 } job_t;
 
-static int pick(const job_t* j, double u) {
-    /* flame.tpl:110-123: first non-zero-weight xform whose running sum reaches u * sum */
-    const double ratio = u * j->wsum;
+static int pick(const job_t* j, int row, double u) {
+    /* flame.tpl:110-123: first non-zero-weight xform whose running sum reaches
+       u * sum, else the last non-zero-weight one (xform 0 when all are zero) */
+    const double ratio = u * j->wsum[row];
     int last_nonzero = 0;
     for (int i = 0; i < j->d->nx; i++) {
-        const double w = j->P[j->d->xf[i].base];
-        if (w != 0.0) {
-            if (i < j->d->nx - 1 && j->cum[i] >= ratio) return i;
+        if (j->wt[row][i] != 0.0) {
+            if (i < j->d->nx - 1 && j->cum[row][i] >= ratio) return i;
             last_nonzero = i;
         }
     }
-    return (j->P[j->d->xf[j->d->nx - 1].base] != 0.0) ? j->d->nx - 1 : last_nonzero;
+    return (j->wt[row][j->d->nx - 1] != 0.0) ? j->d->nx - 1 : last_nonzero;
 }
 
 static void* render_job(void* arg) {
@@ -379,10 +382,12 @@ static void* render_job(void* arg) {
         double c = u01(&r);
         const double* jit = j->jitter + 2 * (ch % (uint64_t)j->n_jitter);
         const uint64_t total = (uint64_t)j->warmup + j->passes;
+        int last = -1; /* previous xform (chaos); none before the first step */
         for (uint64_t pass = 0; pass < total; pass++) {
             for (int k = 0; k < 40; k++) u[k] = u01(&r);
             int used = 1;
-            const int xi = pick(j, u[0]);
+            const int xi = pick(j, d->chaos && last >= 0 ? 1 + last : 0, u[0]);
+            last = xi;
             double op = apply_xf(d, P, xi, &x, &y, &c, u, &used);
             /* refactor.cu:195-199 */
             if (isnan(x) || x > 1e10 || x < -1e10 || isnan(y) || y > 1e10 || y < -1e10) {
@@ -418,7 +423,7 @@ uint64_t oracle_render(const int* structure, const double* params, const double*
                        uint64_t n_chains, uint32_t warmup, uint64_t passes, uint64_t seed, int threads, int n_jitter,
                        const double* jitter_in, int hammersley, double* hist) {
     flame_desc* d = (flame_desc*)malloc(sizeof(flame_desc));
-    if (!d || parse_structure(structure, d) < 0 || d->chaos) {
+    if (!d || parse_structure(structure, d) < 0) {
         free(d);
         return 0;
     }
@@ -442,8 +447,6 @@ uint64_t oracle_render(const int* structure, const double* params, const double*
     job_t* jobs = (job_t*)calloc((size_t)threads, sizeof(job_t));
     pthread_t* tid = (pthread_t*)calloc((size_t)threads, sizeof(pthread_t));
     const size_t hsz = (size_t)w * h * 4;
-    double wsum = 0.0;
-    for (int i = 0; i < d->nx; i++) wsum += params[d->xf[i].base];
     for (int t = 0; t < threads; t++) {
         job_t* j = &jobs[t];
         j->d = d;
@@ -461,11 +464,17 @@ uint64_t oracle_render(const int* structure, const double* params, const double*
         j->n_chains = n_chains;
         j->hammersley = hammersley;
         j->hist = (t == 0) ? hist : (double*)calloc(hsz, sizeof(double));
-        j->wsum = wsum;
-        double run = 0.0;
-        for (int i = 0; i < d->nx; i++) {
-            run += params[d->xf[i].base];
-            j->cum[i] = run;
+        const int rows = d->chaos ? 1 + d->nx : 1;
+        for (int row = 0; row < rows; row++) {
+            double run = 0.0;
+            for (int i = 0; i < d->nx; i++) {
+                double wv = params[d->xf[i].base];
+                if (row > 0) wv *= params[13 + (size_t)(row - 1) * (d->nx + 1) + 1 + i];
+                j->wt[row][i] = wv;
+                run += wv;
+                j->cum[row][i] = run;
+            }
+            j->wsum[row] = run;
         }
     }
     memset(hist, 0, hsz * sizeof(double));

@@ -99,9 +99,12 @@ struct rfk_state {
 
 namespace {
 
+// Floats of a prepared parameter block: the reals (padded to even), the alias
+// pick table (2 per xform, and 2 per xform pair with chaos), the palette
+// (RFK_SAMPLE_FLOATS of rfk_iterate.cuh).
 size_t sample_floats_for(const rfk::generated_flame& g) {
-    size_t off = g.size_reals + g.num_xforms + 1;
-    if (g.chaos) off += g.num_xforms * g.num_xforms + g.num_xforms;
+    size_t off = (g.size_reals + 1) / 2 * 2 + 2 * g.num_xforms;
+    if (g.chaos) off += 2 * g.num_xforms * g.num_xforms;
     off = (off + 3) / 4 * 4;
     return off + 1024;
 }
@@ -119,12 +122,15 @@ std::vector<char> nvrtc_build(const std::string& source, const std::string& arch
     const std::string d_cpt = "-DRFK_CPT=" + std::to_string(cpt);
     const std::string d_flush = "-DRFK_FLUSH=" + std::to_string(flush);
     const std::string d_sort = "-DRFK_SORT=" + std::to_string(sort);
-    // blocks_per_sm > 0 also asks the compiler to fit that many bin blocks per
-    // SM (registers capped through the launch bounds)
-    const std::string d_minb = "-DRFK_MINB=" + std::to_string(o.blocks_per_sm);
+    // the compiler fits blocks_per_sm bin blocks per SM (registers capped
+    // through the launch bounds); by default 40 resident warps: left alone,
+    // it keeps kernel arguments and flame parameters in registers (about 80
+    // per thread) and fewer blocks run
+    const int minb = o.blocks_per_sm > 0 ? o.blocks_per_sm : std::max(1, 1280 / block);
+    const std::string d_minb = "-DRFK_MINB=" + std::to_string(minb);
     std::vector<const char*> opts = {arch.c_str(), "-std=c++17", "-lineinfo", d_block.c_str(), d_cpt.c_str(),
                                      d_flush.c_str(), d_sort.c_str(), "-extra-device-vectorization"};
-    if (o.blocks_per_sm > 0) opts.push_back(d_minb.c_str());
+    opts.push_back(d_minb.c_str());
     if (verbose) opts.push_back("--ptxas-options=-v");  // per-kernel registers / spills / shared memory in the log
     if (!o.precise_math) {
         opts.push_back("--use_fast_math");
@@ -153,11 +159,11 @@ std::vector<char> nvrtc_build(const std::string& source, const std::string& arch
 }
 
 // Sorting chains by xform pays off when there is more than one xform and the
-// per-xform ballots stay few (sort = 0 in the options means this choice).
+// per-xform ballots stay few; sort = 0 in the options means the block sort.
 int resolve_sort(const rfk_compile_opts& o, size_t nx) {
     const bool can = nx >= 2 && nx <= 32;
     if (o.sort < 0 || !can) return 0;
-    return o.sort == 2 ? 2 : 1;
+    return o.sort == 1 ? 1 : 2;
 }
 
 int resolve_cpt(const rfk_compile_opts& o, int sort) {
@@ -895,8 +901,8 @@ rfk_status rfk_autotune(const rfk_db* db, const rfk_flame* f, const double* samp
             }
         }
         struct cand { int block, cpt, flush, sort, minb; };
-        const cand cands[] = {{256, 4, 0, 2, 0}, {256, 4, 1, 2, 0}, {256, 4, 2, 2, 0}, {256, 4, 3, 2, 0},
-                              {256, 4, 1, 1, 0}, {512, 2, 0, 2, 0}, {256, 4, 0, 2, 5}, {256, 4, 1, 2, 5}};
+        const cand cands[] = {{256, 4, 1, 2, 5}, {256, 2, 1, 2, 6}, {256, 8, 1, 2, 4}, {256, 4, 2, 2, 5},
+                              {512, 2, 1, 2, 3}, {128, 4, 1, 2, 12}, {256, 4, 0, 2, 5}, {256, 4, 1, 1, 5}};
         double best_rate = -1.0, worst_rate = 1e300;
         int n = 0;
         for (const cand& c : cands) {

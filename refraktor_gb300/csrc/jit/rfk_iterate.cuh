@@ -44,12 +44,12 @@
 #define RFK_SORT 0
 #endif
 
-// Per-sample parameter block (floats).
-#define RFK_OFF_CUM (RFK_SIZE_REALS)
-#define RFK_OFF_FB (RFK_OFF_CUM + RFK_NX)
-#define RFK_OFF_CCUM (RFK_OFF_FB + 1)
-#define RFK_OFF_CFB (RFK_OFF_CCUM + (RFK_CHAOS ? RFK_NX * RFK_NX : 0))
-#define RFK_OFF_PAL_RAW (RFK_OFF_CFB + (RFK_CHAOS ? RFK_NX : 0))
+// Per-sample parameter block (floats): the reals, the xform pick table (an
+// alias table of RFK_NX (threshold, alias) pairs), with chaos one alias table
+// per previous xform, then the 256 x float4 palette.
+#define RFK_OFF_ALIAS ((RFK_SIZE_REALS + 1) / 2 * 2)
+#define RFK_OFF_CALIAS (RFK_OFF_ALIAS + 2 * RFK_NX)
+#define RFK_OFF_PAL_RAW (RFK_OFF_CALIAS + (RFK_CHAOS ? 2 * RFK_NX * RFK_NX : 0))
 #define RFK_OFF_PAL (((RFK_OFF_PAL_RAW) + 3) / 4 * 4)
 #define RFK_SAMPLE_FLOATS (RFK_OFF_PAL + 1024)
 
@@ -87,6 +87,60 @@ struct rfk_chains {
     float* c;
     unsigned char* last;  // previous xform (chaos), 255 = none
 };
+
+// Walker / Vose alias table of the weights wt[0..RFK_NX): entry i holds a
+// threshold and an alias; a uniform u picks i = floor(u * RFK_NX) and keeps i
+// when the fraction u * RFK_NX - i is below the threshold, else takes the
+// alias, so xform k comes out with probability wt[k] / sum(wt) in O(1)
+// (flame.tpl:110-123 picks by a linear search of the cumulative weights with
+// the same distribution). Zero weights get threshold 0 and the heaviest xform
+// as alias, so they are never picked; all weights zero picks xform 0, as the
+// reference's fallback does.
+__device__ void rfk_alias_table(const float (&wt)[RFK_NX], float* tbl) {
+    float sum = 0.0f;
+    int heavy = 0;
+    for (int i = 0; i < RFK_NX; i++) {
+        sum += wt[i];
+        if (wt[i] > wt[heavy]) heavy = i;
+    }
+    if (!(sum > 0.0f)) {
+        for (int i = 0; i < RFK_NX; i++) {
+            tbl[2 * i] = 0.0f;
+            tbl[2 * i + 1] = __int_as_float(0);
+        }
+        return;
+    }
+    float q[RFK_NX];
+    int small[RFK_NX], large[RFK_NX];
+    int ns = 0, nl = 0;
+    for (int i = 0; i < RFK_NX; i++) {
+        q[i] = wt[i] * (float)RFK_NX / sum;
+        if (q[i] < 1.0f) small[ns++] = i;
+        else large[nl++] = i;
+    }
+    while (ns > 0 && nl > 0) {
+        const int sm = small[--ns], lg = large[nl - 1];
+        tbl[2 * sm] = q[sm];
+        tbl[2 * sm + 1] = __int_as_float(lg);
+        q[lg] = (q[lg] + q[sm]) - 1.0f;
+        if (q[lg] < 1.0f) {
+            nl--;
+            small[ns++] = lg;
+        }
+    }
+    // what rounding leaves over keeps itself (zero weights: the heaviest)
+    while (nl > 0) {
+        const int lg = large[--nl];
+        tbl[2 * lg] = 2.0f;
+        tbl[2 * lg + 1] = __int_as_float(lg);
+    }
+    while (ns > 0) {
+        const int sm = small[--ns];
+        const bool zero = !(wt[sm] > 0.0f);
+        tbl[2 * sm] = zero ? 0.0f : 2.0f;
+        tbl[2 * sm + 1] = __int_as_float(zero ? heavy : sm);
+    }
+}
 
 // ---------------------------------------------------------------- prepare --
 // One block per temporal sample: evaluate the spline segment at t, convert
@@ -149,37 +203,22 @@ extern "C" __global__ void __launch_bounds__(256) rfk_prepare(const float4* __re
         Rng rng;
         rng.start(s, 0xFFFFu, 0xFFFFFFFFFFFFFFFFull, seed, salt);
         // weight sum and pick table (flame.tpl:110-123 semantics)
+        float wt[RFK_NX];
         float wsum = 0.0f;
-        for (int i = 0; i < RFK_NX; i++) wsum += P[rfk_xf_base[i]];
-        P[12] = wsum;
-        float run = 0.0f;
-        int last_nonzero = 0;
         for (int i = 0; i < RFK_NX; i++) {
-            float w = P[rfk_xf_base[i]];
-            run += w;
-            P[RFK_OFF_CUM + i] = (w != 0.0f) ? run : -1.0f;
-            if (w != 0.0f) last_nonzero = i;
+            wt[i] = P[rfk_xf_base[i]];
+            wsum += wt[i];
         }
-        P[RFK_OFF_FB] = __int_as_float(last_nonzero);
+        P[12] = wsum;
+        rfk_alias_table(wt, P + RFK_OFF_ALIAS);
 #if RFK_CHAOS
-        // chaos rows (flame.tpl:170-177): weights[j] *= xform_j.weight
+        // chaos rows (flame.tpl:170-177): weights[j] *= xform_j.weight; the
+        // interpolated rows themselves stay as they are
         for (int r = 0; r < RFK_NX; r++) {
             const unsigned row = 13 + r * (RFK_NX + 1);
-            float rs = 0.0f;
-            for (int j = 0; j < RFK_NX; j++) {
-                P[row + 1 + j] *= P[rfk_xf_base[j]];
-                rs += P[row + 1 + j];
-            }
-            P[row] = rs;
-            float rr = 0.0f;
-            int ln = 0;
-            for (int j = 0; j < RFK_NX; j++) {
-                float w = P[row + 1 + j];
-                rr += w;
-                P[RFK_OFF_CCUM + r * RFK_NX + j] = (w != 0.0f) ? rr : -1.0f;
-                if (w != 0.0f) ln = j;
-            }
-            P[RFK_OFF_CFB + r] = __int_as_float(ln);
+            float rw[RFK_NX];
+            for (int j = 0; j < RFK_NX; j++) rw[j] = P[row + 1 + j] * wt[j];
+            rfk_alias_table(rw, P + RFK_OFF_CALIAS + r * (2 * RFK_NX));
         }
 #endif
         // screen jitter ~ gauss(1/3 px) for antialiasing (flame.tpl:179-182)
@@ -196,24 +235,17 @@ extern "C" __global__ void __launch_bounds__(256) rfk_prepare(const float4* __re
 }
 
 // ------------------------------------------------------------- chain step --
+// Xform pick from a uniform u in [0, 1) through the alias table (of the
+// previous xform's chaos row when there is one).
 __device__ __forceinline__ int rfk_pick(float u, const float* __restrict__ P, unsigned last) {
+    const float* tbl = P + RFK_OFF_ALIAS;
 #if RFK_CHAOS
-    if (last != 255u) {
-        const float ratio = u * P[13 + last * (RFK_NX + 1)];
-        const float* cum = P + RFK_OFF_CCUM + last * RFK_NX;
-        int k = __float_as_int(P[RFK_OFF_CFB + last]);
-#pragma unroll
-        for (int i = RFK_NX - 2; i >= 0; i--)
-            if (cum[i] >= ratio) k = i;
-        return k;
-    }
+    if (last != 255u) tbl = P + RFK_OFF_CALIAS + last * (2 * RFK_NX);
 #endif
-    const float ratio = u * P[12];
-    int k = __float_as_int(P[RFK_OFF_FB]);
-#pragma unroll
-    for (int i = RFK_NX - 2; i >= 0; i--)
-        if (P[RFK_OFF_CUM + i] >= ratio) k = i;
-    return k;
+    const float v = u * (float)RFK_NX;
+    const int i = min((int)v, RFK_NX - 1);
+    const float2 e = reinterpret_cast<const float2*>(tbl)[i];
+    return (v - (float)i < e.x) ? i : __float_as_int(e.y);
 }
 
 // Moves one chain through xform k: apply, bad-value reset, final xform on a
@@ -271,16 +303,17 @@ __device__ __forceinline__ int rfk_step(float& x, float& y, float& c, unsigned& 
 }
 
 #if RFK_SORT
-// Counting sort of a warp's 32 * RFK_CPT chains by their picked xform,
-// through the warp's stage buffer in shared memory: afterwards round q of
-// every lane holds sorted slot q * 32 + lane, so the lanes of one round run
-// the same xform except at the boundaries between xform runs. Each round's
-// lanes with equal xform are grouped by __match_any_sync; the group leader
-// reserves the group's places in the per-warp xform counters; a warp scan of
-// the counters gives each xform's start. Only __syncwarp is needed.
-__device__ __forceinline__ void rfk_sort_chains(float (&x)[RFK_CPT], float (&y)[RFK_CPT], float (&c)[RFK_CPT],
-                                                int (&k)[RFK_CPT], float4* __restrict__ stage,
-                                                unsigned* __restrict__ counts) {
+// Counting sort of a warp's 32 * RFK_CPT chains by their picked xform, in
+// place in the warp's region of the chain array: the caller has read every
+// slot of the warp (its values v and picks k) before the call, so the scatter
+// may overwrite any of them. Afterwards slot q * 32 + lane of the region holds
+// the lane's round-q chain, and the lanes of one round run the same xform
+// except at the boundaries between xform runs. Each round's lanes with equal
+// xform are grouped by __match_any_sync; the group leader reserves the group's
+// places in the per-warp xform counters; a warp scan of the counters gives
+// each xform's start. Only __syncwarp is needed.
+__device__ __forceinline__ void rfk_sort_chains(float4* __restrict__ region, const float4 (&v)[RFK_CPT],
+                                                const int (&k)[RFK_CPT], unsigned* __restrict__ counts) {
     const unsigned lane = threadIdx.x & 31u;
     const unsigned lt = (1u << lane) - 1u;
     if (lane < RFK_NX) counts[lane] = 0u;
@@ -300,39 +333,33 @@ __device__ __forceinline__ void rfk_sort_chains(float (&x)[RFK_CPT], float (&y)[
     unsigned incl = cnt;
 #pragma unroll
     for (int d = 1; d < 32; d <<= 1) {
-        const unsigned v = __shfl_up_sync(0xffffffffu, incl, d);
-        if ((int)lane >= d) incl += v;
+        const unsigned u = __shfl_up_sync(0xffffffffu, incl, d);
+        if ((int)lane >= d) incl += u;
     }
     const unsigned start = incl - cnt;
 #pragma unroll
     for (int q = 0; q < RFK_CPT; q++) {
         const unsigned pos = __shfl_sync(0xffffffffu, start, k[q]) + off[q];
-        stage[pos] = make_float4(x[q], y[q], c[q], __int_as_float(k[q]));
-    }
-    __syncwarp();
-#pragma unroll
-    for (int q = 0; q < RFK_CPT; q++) {
-        const float4 v = stage[q * 32 + lane];
-        x[q] = v.x;
-        y[q] = v.y;
-        c[q] = v.z;
-        k[q] = __float_as_int(v.w);
+        region[pos] = make_float4(v[q].x, v[q].y, v[q].z, __int_as_float(k[q]));
     }
     __syncwarp();
 }
 
 #define RFK_NW (RFK_BLOCK / 32)
 // Block-wide counting sort of the block's RFK_BLOCK * RFK_CPT chains by picked
-// xform (deterministic order: xform-major, then warp, then round, then lane).
+// xform (deterministic order: xform-major, then warp, then round, then lane),
+// in place in the chain array: every thread has read its own slots (values v,
+// picks k) before the call, and the scatter comes after two barriers.
 // counts[RFK_NX * RFK_NW] must be zero on entry; it is used in place for the
 // starts. `next` (the other counter set) is cleared between the first and the
 // second barrier: every thread finished the previous pass's reads of it before
 // the first barrier, and every thread's next-pass updates of it come after the
-// second. Afterwards thread t holds sorted slots q * RFK_BLOCK + t, so a warp's
-// round covers 32 consecutive slots of one xform run except at run ends.
-__device__ __forceinline__ void rfk_block_sort(float (&x)[RFK_CPT], float (&y)[RFK_CPT], float (&c)[RFK_CPT],
-                                               int (&k)[RFK_CPT], float4* __restrict__ stage,
-                                               unsigned* __restrict__ counts, unsigned* __restrict__ next) {
+// second. Afterwards slot q * RFK_BLOCK + t holds thread t's round-q chain, so
+// a warp's round covers 32 consecutive slots of one xform run except at run
+// ends.
+__device__ __forceinline__ void rfk_block_sort(float4* __restrict__ chains, const float4 (&v)[RFK_CPT],
+                                               const int (&k)[RFK_CPT], unsigned* __restrict__ counts,
+                                               unsigned* __restrict__ next) {
     const unsigned lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
     const unsigned lt = (1u << lane) - 1u;
     unsigned off[RFK_CPT];
@@ -361,8 +388,8 @@ __device__ __forceinline__ void rfk_block_sort(float (&x)[RFK_CPT], float (&y)[R
         unsigned incl = sum;
 #pragma unroll
         for (int d = 1; d < 32; d <<= 1) {
-            const unsigned v = __shfl_up_sync(0xffffffffu, incl, d);
-            if ((int)lane >= d) incl += v;
+            const unsigned u = __shfl_up_sync(0xffffffffu, incl, d);
+            if ((int)lane >= d) incl += u;
         }
         unsigned run = incl - sum;
 #pragma unroll
@@ -376,17 +403,9 @@ __device__ __forceinline__ void rfk_block_sort(float (&x)[RFK_CPT], float (&y)[R
 #pragma unroll
     for (int q = 0; q < RFK_CPT; q++) {
         const unsigned pos = counts[k[q] * RFK_NW + warp] + off[q];
-        stage[pos] = make_float4(x[q], y[q], c[q], __int_as_float(k[q]));
+        chains[pos] = make_float4(v[q].x, v[q].y, v[q].z, __int_as_float(k[q]));
     }
     __syncthreads();
-#pragma unroll
-    for (int q = 0; q < RFK_CPT; q++) {
-        const float4 v = stage[q * RFK_BLOCK + threadIdx.x];
-        x[q] = v.x;
-        y[q] = v.y;
-        c[q] = v.z;
-        k[q] = __float_as_int(v.w);
-    }
 }
 #endif
 
@@ -512,35 +531,18 @@ struct rfk_bin_args {
     unsigned slice;                     // passes per temporal sample before switching (rfk_bin_tm)
 };
 
-// Rotates the per-lane chain slots by one (slot q takes slot q + 1), with
-// register moves only.
-template <typename T0, typename T1>
-__device__ __forceinline__ void rfk_rot1(T0 (&a)[RFK_CPT], T1 (&b)[RFK_CPT]) {
-    const T0 a0 = a[0];
-    const T1 b0 = b[0];
-#pragma unroll
-    for (int q = 0; q + 1 < RFK_CPT; q++) {
-        a[q] = a[q + 1];
-        b[q] = b[q + 1];
-    }
-    a[RFK_CPT - 1] = a0;
-    b[RFK_CPT - 1] = b0;
-}
-
-__device__ __forceinline__ void rfk_rotate(float (&x)[RFK_CPT], float (&y)[RFK_CPT], float (&c)[RFK_CPT], int (&k)[RFK_CPT],
-                                           unsigned (&last)[RFK_CPT], unsigned (&chain)[RFK_CPT]) {
-    rfk_rot1(x, y);
-    rfk_rot1(c, k);
-    rfk_rot1(last, chain);
-}
-
-// Shared memory of a block's passes: sort staging and the hot-pixel cache.
+// Shared memory of a block's passes: the block's chains, the sort counters
+// and the hot-pixel cache. Chain slot q of thread t holds (x, y, colour,
+// last xform as int bits; 255 = none) at rfk_slot(q): q * RFK_BLOCK + t, or,
+// with the warp sort, q * 32 + lane within the warp's region. Keeping the
+// chains in shared memory rather than in per-thread register arrays leaves
+// only the moving chain in registers (about a third fewer registers per
+// thread, more resident warps) and needs no register rotation between slots.
 struct rfk_pass_smem {
+    float4 chains[RFK_BLOCK * RFK_CPT];
 #if RFK_SORT == 1
-    float4 stage[RFK_BLOCK / 32][32 * RFK_CPT];
     unsigned counts[RFK_BLOCK / 32][32];
 #elif RFK_SORT == 2
-    float4 stage[RFK_BLOCK * RFK_CPT];
     unsigned counts[2][RFK_NX * (RFK_BLOCK / 32)];  // ping-pong sets, one per pass parity
 #endif
 #if RFK_FLUSH >= 2
@@ -548,6 +550,14 @@ struct rfk_pass_smem {
 #endif
     unsigned dummy;
 };
+
+__device__ __forceinline__ unsigned rfk_slot(int q) {
+#if RFK_SORT == 1
+    return (threadIdx.x & ~31u) * RFK_CPT + (unsigned)q * 32u + (threadIdx.x & 31u);
+#else
+    return (unsigned)q * RFK_BLOCK + threadIdx.x;
+#endif
+}
 
 // All threads of the block, once, before the first pass.
 __device__ __forceinline__ void rfk_pass_smem_init(rfk_pass_smem& sm) {
@@ -559,6 +569,37 @@ __device__ __forceinline__ void rfk_pass_smem_init(rfk_pass_smem& sm) {
 #endif
 }
 
+// This thread's chains chain0 + q * cstride (q < RFK_CPT) from the state
+// arrays into its slots, and back. Only the thread's own slots are touched.
+__device__ __forceinline__ void rfk_load_chains(rfk_pass_smem& sm, const rfk_chains& st, unsigned chain0,
+                                                unsigned cstride) {
+#pragma unroll
+    for (int q = 0; q < RFK_CPT; q++) {
+        const unsigned id = chain0 + (unsigned)q * cstride;
+#if RFK_CHAOS
+        const unsigned last = st.last[id];
+#else
+        const unsigned last = 255u;
+#endif
+        sm.chains[rfk_slot(q)] = make_float4(st.x[id], st.y[id], st.c[id], __int_as_float((int)last));
+    }
+}
+
+__device__ __forceinline__ void rfk_store_chains(const rfk_pass_smem& sm, const rfk_chains& st, unsigned chain0,
+                                                 unsigned cstride) {
+#pragma unroll
+    for (int q = 0; q < RFK_CPT; q++) {
+        const unsigned id = chain0 + (unsigned)q * cstride;
+        const float4 v = sm.chains[rfk_slot(q)];
+        st.x[id] = v.x;
+        st.y[id] = v.y;
+        st.c[id] = v.z;
+#if RFK_CHAOS
+        st.last[id] = (unsigned char)__float_as_int(v.w);
+#endif
+    }
+}
+
 #if RFK_FLUSH >= 2
 #define RFK_CACHE_ARG , sm.cache
 #else
@@ -566,68 +607,69 @@ __device__ __forceinline__ void rfk_pass_smem_init(rfk_pass_smem& sm) {
 #endif
 
 // One pass over this thread's RFK_CPT chains, in two parts with the loop over
-// chain slots in the kernel body:
+// slots in the kernel body:
 //   rfk_pick_sort  every thread of the block (the block sort synchronises):
-//                  picks of this lane's chains from one Philox stream per lane
-//                  (lane_stream, call_id, pass), then the sort by xform;
-//   rfk_move_slot  RFK_CPT times: the chain in slot 0 moves (Philox stream of
-//                  the slot, call_id, pass) and draws unless `draw` is false
-//                  (warm-up), then the slots rotate by one. Its pointers carry
-//                  no __restrict__: with it the compiler kept the flame
+//                  picks of this thread's chains from one Philox stream per
+//                  lane (lane_stream, call_id, pass), then the sort by xform,
+//                  which leaves each slot's pick in its last-xform field;
+//   rfk_move_slot  for q < RFK_CPT: the chain in slot q moves (Philox stream
+//                  of the slot's chain id, call_id, pass) and draws unless
+//                  `draw` is false (warm-up). Its pointers carry no
+//                  __restrict__: with it the compiler kept the flame
 //                  parameters in registers across the loop (about 155
 //                  registers per thread instead of 60, a quarter of the
 //                  occupancy).
 // Without sorting (RFK_SORT 0) rfk_pick_sort does nothing and rfk_move_slot
-// picks and moves the chain in slot 0.
-__device__ __forceinline__ void rfk_pick_sort(float (&x)[RFK_CPT], float (&y)[RFK_CPT], float (&c)[RFK_CPT],
-                                              const unsigned (&last)[RFK_CPT], int (&kk)[RFK_CPT], rfk_pass_smem& sm,
-                                              const float* P, unsigned lane_stream, unsigned call_id,
-                                              unsigned long long pass, unsigned seed, unsigned salt) {
+// picks and moves the chain in slot q.
+__device__ __forceinline__ void rfk_pick_sort(rfk_pass_smem& sm, const float* P, unsigned lane_stream,
+                                              unsigned call_id, unsigned long long pass, unsigned seed,
+                                              unsigned salt) {
 #if RFK_SORT
     Rng pr;
     pr.start_lazy(lane_stream, call_id, pass, seed, salt ^ 0x9E3779B9u);
+    float4 v[RFK_CPT];
+    int kk[RFK_CPT];
 #pragma unroll
-    for (int k = 0; k < RFK_CPT; k++) kk[k] = rfk_pick(pr.u01(), P, last[k]);
+    for (int q = 0; q < RFK_CPT; q++) {
+        v[q] = sm.chains[rfk_slot(q)];
+        kk[q] = rfk_pick(pr.u01(), P, (unsigned)__float_as_int(v[q].w));
+    }
 #if RFK_SORT == 2
-    rfk_block_sort(x, y, c, kk, sm.stage, sm.counts[pass & 1], sm.counts[(pass + 1) & 1]);
+    rfk_block_sort(sm.chains, v, kk, sm.counts[pass & 1], sm.counts[(pass + 1) & 1]);
 #else
-    rfk_sort_chains(x, y, c, kk, sm.stage[threadIdx.x >> 5], sm.counts[threadIdx.x >> 5]);
+    rfk_sort_chains(sm.chains + (threadIdx.x & ~31u) * RFK_CPT, v, kk, sm.counts[threadIdx.x >> 5]);
 #endif
 #else
-    (void)x; (void)y; (void)c; (void)last; (void)sm; (void)P; (void)lane_stream; (void)call_id; (void)pass;
-    (void)seed; (void)salt;
-#pragma unroll
-    for (int k = 0; k < RFK_CPT; k++) kk[k] = 0;
+    (void)sm; (void)P; (void)lane_stream; (void)call_id; (void)pass; (void)seed; (void)salt;
 #endif
 }
 
-__device__ __forceinline__ void rfk_move_slot(float (&x)[RFK_CPT], float (&y)[RFK_CPT], float (&c)[RFK_CPT],
-                                              int (&kk)[RFK_CPT], unsigned (&last)[RFK_CPT], unsigned (&chain)[RFK_CPT],
-                                              rfk_pass_smem& sm, const float* P, float4* bins,
+__device__ __forceinline__ void rfk_move_slot(int q, unsigned chain, rfk_pass_smem& sm, const float* P, float4* bins,
                                               unsigned w, unsigned h, unsigned call_id, unsigned long long pass,
                                               unsigned seed, unsigned salt, bool draw, unsigned& my_hits,
                                               unsigned& my_draws) {
+    float4* slot = &sm.chains[rfk_slot(q)];
+    const float4 s = *slot;
+    float x = s.x, y = s.y, c = s.z;
+    unsigned last = (unsigned)__float_as_int(s.w);
     float4 v;
     unsigned hit;
     int idx;
+    Rng rng;
 #if RFK_SORT
-#if RFK_CHAOS
-    last[0] = (unsigned)kk[0];
-#endif
-    Rng rng;
-    rng.start_lazy(chain[0], call_id, pass, seed, salt);
-    idx = rfk_move(kk[0], x[0], y[0], c[0], rng, P, w, h, v, hit);
+    // the sort left this slot's pick in the last-xform field
+    rng.start_lazy(chain, call_id, pass, seed, salt);
+    idx = rfk_move((int)last, x, y, c, rng, P, w, h, v, hit);
 #else
-    Rng rng;
-    rng.start(chain[0], call_id, pass, seed, salt);
-    idx = rfk_step(x[0], y[0], c[0], last[0], rng, P, w, h, v, hit);
+    rng.start(chain, call_id, pass, seed, salt);
+    idx = rfk_step(x, y, c, last, rng, P, w, h, v, hit);
 #endif
+    *slot = make_float4(x, y, c, __int_as_float((int)last));
     if (draw) {
         rfk_flush(bins, idx, v RFK_CACHE_ARG);
         my_hits += hit;
         my_draws += (idx >= 0) ? 1u : 0u;
     }
-    rfk_rotate(x, y, c, kk, last, chain);
 }
 
 // Block totals of the check interval: warp sums, then shared atomics. Ends
@@ -675,21 +717,9 @@ extern "C" __global__ void RFK_BIN_BOUNDS rfk_bin(rfk_bin_args a) {
         s_start = rfk_time();
         atomicMin(&a.counters->start_ns, s_start);
     }
-    float x[RFK_CPT], y[RFK_CPT], c[RFK_CPT];
-    unsigned last[RFK_CPT];
-    unsigned chain[RFK_CPT];
-#pragma unroll
-    for (int k = 0; k < RFK_CPT; k++) {
-        chain[k] = (k * gridDim.x + blockIdx.x) * RFK_BLOCK + threadIdx.x;
-        x[k] = a.st.x[chain[k]];
-        y[k] = a.st.y[chain[k]];
-        c[k] = a.st.c[chain[k]];
-#if RFK_CHAOS
-        last[k] = a.st.last[chain[k]];
-#else
-        last[k] = 255u;
-#endif
-    }
+    // chain of slot q: chain0 + q * cstride
+    const unsigned chain0 = blockIdx.x * RFK_BLOCK + threadIdx.x, cstride = gridDim.x * RFK_BLOCK;
+    rfk_load_chains(sm, a.st, chain0, cstride);
     __syncthreads();
 
     unsigned long long pass = 0;
@@ -698,12 +728,11 @@ extern "C" __global__ void RFK_BIN_BOUNDS rfk_bin(rfk_bin_args a) {
     for (;;) {
 #pragma unroll 1
         for (unsigned it = 0; it < a.check && (a.max_passes == 0 || pass < a.max_passes); it++) {
-            int kk[RFK_CPT];
-            rfk_pick_sort(x, y, c, last, kk, sm, P, lane_stream, a.call_id, pass, a.seed, a.salt);
+            rfk_pick_sort(sm, P, lane_stream, a.call_id, pass, a.seed, a.salt);
 #pragma unroll 1
-            for (int k = 0; k < RFK_CPT; k++)
-                rfk_move_slot(x, y, c, kk, last, chain, sm, P, a.bins, a.w, a.h, a.call_id, pass, a.seed, a.salt, true,
-                              my_hits, my_draws);
+            for (int q = 0; q < RFK_CPT; q++)
+                rfk_move_slot(q, chain0 + (unsigned)q * cstride, sm, P, a.bins, a.w, a.h, a.call_id, pass, a.seed,
+                              a.salt, true, my_hits, my_draws);
             pass++;
         }
         // bailout check: block totals -> global counters -> decision
@@ -728,15 +757,7 @@ extern "C" __global__ void RFK_BIN_BOUNDS rfk_bin(rfk_bin_args a) {
         __syncthreads();
         if (s_bail) break;
     }
-#pragma unroll
-    for (int k = 0; k < RFK_CPT; k++) {
-        a.st.x[chain[k]] = x[k];
-        a.st.y[chain[k]] = y[k];
-        a.st.c[chain[k]] = c[k];
-#if RFK_CHAOS
-        a.st.last[chain[k]] = (unsigned char)last[k];
-#endif
-    }
+    rfk_store_chains(sm, a.st, chain0, cstride);
     if (threadIdx.x == 0) {
         atomicAdd(&a.counters->passes, pass * (unsigned long long)(RFK_BLOCK * RFK_CPT));
         atomicOr(&a.counters->status, s_bail);
@@ -762,46 +783,34 @@ extern "C" __global__ void RFK_BIN_BOUNDS rfk_warmup(const float* __restrict__ s
     __syncthreads();
     const unsigned total = gridDim.x * RFK_BLOCK * RFK_CPT;
     const unsigned lane_stream = blockIdx.x * RFK_BLOCK + threadIdx.x;
-    float x[RFK_CPT], y[RFK_CPT], c[RFK_CPT];
-    unsigned last[RFK_CPT], chain[RFK_CPT];
+    const unsigned chain0 = blockIdx.x * RFK_BLOCK + threadIdx.x, cstride = gridDim.x * RFK_BLOCK;
 #pragma unroll
-    for (int k = 0; k < RFK_CPT; k++) {
-        chain[k] = (k * gridDim.x + blockIdx.x) * RFK_BLOCK + threadIdx.x;
+    for (int q = 0; q < RFK_CPT; q++) {
+        const unsigned chain = chain0 + (unsigned)q * cstride;
         Rng rng;
-        rng.start(chain[k], 0xFFFDu, 0ull, seed, salt);
-        const V2 pos = rfk_hammersley(chain[k], total);
+        rng.start(chain, 0xFFFDu, 0ull, seed, salt);
+        const V2 pos = rfk_hammersley(chain, total);
         const float px = (pos.x + 1.0f) / 2.0f * (float)w;
         const float py = (pos.y + 1.0f) / 2.0f * (float)h;
         // plane-space affine at P[6..11]
-        x[k] = fmaf(P[6], px, fmaf(P[8], py, P[10]));
-        y[k] = fmaf(P[7], px, fmaf(P[9], py, P[11]));
-        c[k] = rng.u01();
-        last[k] = 255u;
+        sm.chains[rfk_slot(q)] = make_float4(fmaf(P[6], px, fmaf(P[8], py, P[10])), fmaf(P[7], px, fmaf(P[9], py, P[11])),
+                                             rng.u01(), __int_as_float(255));
     }
     unsigned no_hits = 0, no_draws = 0;
 #pragma unroll 1
     for (unsigned pass = 0; pass < warmup_count; pass++) {
-        int kk[RFK_CPT];
-        rfk_pick_sort(x, y, c, last, kk, sm, P, lane_stream, 0xFFFEu, pass, seed, salt);
+        rfk_pick_sort(sm, P, lane_stream, 0xFFFEu, pass, seed, salt);
 #pragma unroll 1
-        for (int k = 0; k < RFK_CPT; k++) {
-            rfk_move_slot(x, y, c, kk, last, chain, sm, P, nullptr, w, h, 0xFFFEu, pass, seed, salt, false, no_hits,
-                          no_draws);
+        for (int q = 0; q < RFK_CPT; q++) {
+            rfk_move_slot(q, chain0 + (unsigned)q * cstride, sm, P, nullptr, w, h, 0xFFFEu, pass, seed, salt, false,
+                          no_hits, no_draws);
             // without the histogram updates (asm with a memory clobber) the
             // compiler would keep the flame parameters in registers across
             // passes: twice the registers, half the occupancy
             asm volatile("" ::: "memory");
         }
     }
-#pragma unroll
-    for (int k = 0; k < RFK_CPT; k++) {
-        st.x[chain[k]] = x[k];
-        st.y[chain[k]] = y[k];
-        st.c[chain[k]] = c[k];
-#if RFK_CHAOS
-        st.last[chain[k]] = (unsigned char)last[k];
-#endif
-    }
+    rfk_store_chains(sm, st, chain0, cstride);
 }
 
 // ------------------------------------------------- temporal multiplier ----
@@ -835,23 +844,12 @@ extern "C" __global__ void RFK_BIN_BOUNDS rfk_bin_tm(rfk_bin_args a) {
         atomicMin(&a.counters->start_ns, s_start);
     }
     for (unsigned i = threadIdx.x; i < RFK_MAX_TMUL; i += RFK_BLOCK) s_q[i] = 0;
-    float x[RFK_CPT], y[RFK_CPT], c[RFK_CPT];
-    unsigned last[RFK_CPT], chain[RFK_CPT];
     int cur = 0;
     unsigned smp = blockIdx.x;
+    // chain of slot q of temporal sample smp: smp * RFK_BLOCK + t + q * cstride
+    const unsigned cstride = S * RFK_BLOCK;
     for (unsigned i = threadIdx.x; i < RFK_SAMPLE_FLOATS; i += RFK_BLOCK) P[i] = a.samples[(size_t)smp * RFK_SAMPLE_FLOATS + i];
-#pragma unroll
-    for (int k = 0; k < RFK_CPT; k++) {
-        chain[k] = (k * S + smp) * RFK_BLOCK + threadIdx.x;
-        x[k] = a.st.x[chain[k]];
-        y[k] = a.st.y[chain[k]];
-        c[k] = a.st.c[chain[k]];
-#if RFK_CHAOS
-        last[k] = a.st.last[chain[k]];
-#else
-        last[k] = 255u;
-#endif
-    }
+    rfk_load_chains(sm, a.st, smp * RFK_BLOCK + threadIdx.x, cstride);
     __syncthreads();
 
     unsigned long long pass = 0, total = 0;
@@ -862,12 +860,12 @@ extern "C" __global__ void RFK_BIN_BOUNDS rfk_bin_tm(rfk_bin_args a) {
         unsigned n = 0;
 #pragma unroll 1
         for (; n < a.check && (a.max_passes == 0 || total < a.max_passes); n++) {
-            int kk[RFK_CPT];
-            rfk_pick_sort(x, y, c, last, kk, sm, P, lane_stream, a.call_id, pass, a.seed, a.salt);
+            rfk_pick_sort(sm, P, lane_stream, a.call_id, pass, a.seed, a.salt);
+            const unsigned chain0 = smp * RFK_BLOCK + threadIdx.x;
 #pragma unroll 1
-            for (int k = 0; k < RFK_CPT; k++)
-                rfk_move_slot(x, y, c, kk, last, chain, sm, P, a.bins, a.w, a.h, a.call_id, pass, a.seed, a.salt, true,
-                              my_hits, my_draws);
+            for (int q = 0; q < RFK_CPT; q++)
+                rfk_move_slot(q, chain0 + (unsigned)q * cstride, sm, P, a.bins, a.w, a.h, a.call_id, pass, a.seed,
+                              a.salt, true, my_hits, my_draws);
             pass++;
             total++;
         }
@@ -906,46 +904,19 @@ extern "C" __global__ void RFK_BIN_BOUNDS rfk_bin_tm(rfk_bin_args a) {
         const int nxt = s_next;
         if (nxt != cur) {
             // park this sample's chains, bring in the next sample
-#pragma unroll
-            for (int k = 0; k < RFK_CPT; k++) {
-                a.st.x[chain[k]] = x[k];
-                a.st.y[chain[k]] = y[k];
-                a.st.c[chain[k]] = c[k];
-#if RFK_CHAOS
-                a.st.last[chain[k]] = (unsigned char)last[k];
-#endif
-            }
+            rfk_store_chains(sm, a.st, smp * RFK_BLOCK + threadIdx.x, cstride);
             cur = nxt;
             smp = blockIdx.x + gridDim.x * (unsigned)cur;
             for (unsigned i = threadIdx.x; i < RFK_SAMPLE_FLOATS; i += RFK_BLOCK)
                 P[i] = a.samples[(size_t)smp * RFK_SAMPLE_FLOATS + i];
-#pragma unroll
-            for (int k = 0; k < RFK_CPT; k++) {
-                chain[k] = (k * S + smp) * RFK_BLOCK + threadIdx.x;
-                x[k] = a.st.x[chain[k]];
-                y[k] = a.st.y[chain[k]];
-                c[k] = a.st.c[chain[k]];
-#if RFK_CHAOS
-                last[k] = a.st.last[chain[k]];
-#else
-                last[k] = 255u;
-#endif
-            }
+            rfk_load_chains(sm, a.st, smp * RFK_BLOCK + threadIdx.x, cstride);
             in_slice = 0;
             __syncthreads();
         } else if (in_slice >= a.slice) {
             in_slice = 0;
         }
     }
-#pragma unroll
-    for (int k = 0; k < RFK_CPT; k++) {
-        a.st.x[chain[k]] = x[k];
-        a.st.y[chain[k]] = y[k];
-        a.st.c[chain[k]] = c[k];
-#if RFK_CHAOS
-        a.st.last[chain[k]] = (unsigned char)last[k];
-#endif
-    }
+    rfk_store_chains(sm, a.st, smp * RFK_BLOCK + threadIdx.x, cstride);
     if (threadIdx.x == 0) {
         atomicAdd(&a.counters->passes, total * (unsigned long long)(RFK_BLOCK * RFK_CPT));
         atomicOr(&a.counters->status, s_bail);
@@ -1025,15 +996,7 @@ extern "C" __global__ void RFK_BIN_BOUNDS rfk_bin_batch(rfk_batch_args a) {
         s_start = rfk_time();
         atomicMin(&a.counters->start_ns, s_start);
     }
-    float x[RFK_CPT], y[RFK_CPT], c[RFK_CPT];
-    unsigned last[RFK_CPT];
-    unsigned chain[RFK_CPT];
-#pragma unroll
-    for (int k = 0; k < RFK_CPT; k++) {
-        chain[k] = (k * gridDim.x + blockIdx.x) * RFK_BLOCK + threadIdx.x;
-        x[k] = y[k] = c[k] = 0.0f;
-        last[k] = 255u;
-    }
+    const unsigned chain0 = blockIdx.x * RFK_BLOCK + threadIdx.x, cstride = gridDim.x * RFK_BLOCK;
     int cur = -1;
     unsigned long long pass = 0;  // the block's running pass count
     unsigned long long total_passes = 0;
@@ -1080,14 +1043,14 @@ extern "C" __global__ void RFK_BIN_BOUNDS rfk_bin_batch(rfk_batch_args a) {
         unsigned warm = 0;
         if (u != cur) {
 #pragma unroll
-            for (int k = 0; k < RFK_CPT; k++) {
+            for (int q = 0; q < RFK_CPT; q++) {
                 Rng r0;
-                r0.start(chain[k], 0xFFFDu, ((unsigned long long)call_id << 32) | (unsigned)item, a.seed, a.salt);
+                r0.start(chain0 + (unsigned)q * cstride, 0xFFFDu, ((unsigned long long)call_id << 32) | (unsigned)item,
+                         a.seed, a.salt);
                 const float px = r0.u01() * (float)U.w, py = r0.u01() * (float)U.h;
-                x[k] = fmaf(P[6], px, fmaf(P[8], py, P[10]));
-                y[k] = fmaf(P[7], px, fmaf(P[9], py, P[11]));
-                c[k] = r0.u01();
-                last[k] = 255u;
+                const float cx = fmaf(P[6], px, fmaf(P[8], py, P[10]));
+                const float cy = fmaf(P[7], px, fmaf(P[9], py, P[11]));
+                sm.chains[rfk_slot(q)] = make_float4(cx, cy, r0.u01(), __int_as_float(255));
             }
             warm = a.warmup;
             cur = u;
@@ -1101,12 +1064,11 @@ extern "C" __global__ void RFK_BIN_BOUNDS rfk_bin_batch(rfk_batch_args a) {
 #pragma unroll 1
             for (unsigned it = 0; it < n; it++) {
                 const bool draw = done + it >= warm;
-                int kk[RFK_CPT];
-                rfk_pick_sort(x, y, c, last, kk, sm, P, lane_stream, call_id, pass, a.seed, a.salt);
+                rfk_pick_sort(sm, P, lane_stream, call_id, pass, a.seed, a.salt);
 #pragma unroll 1
-                for (int k = 0; k < RFK_CPT; k++)
-                    rfk_move_slot(x, y, c, kk, last, chain, sm, P, U.bins, U.w, U.h, call_id, pass, a.seed, a.salt, draw,
-                                  my_hits, my_draws);
+                for (int q = 0; q < RFK_CPT; q++)
+                    rfk_move_slot(q, chain0 + (unsigned)q * cstride, sm, P, U.bins, U.w, U.h, call_id, pass, a.seed,
+                                  a.salt, draw, my_hits, my_draws);
                 pass++;
             }
             done += n;

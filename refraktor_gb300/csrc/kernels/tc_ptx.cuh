@@ -151,6 +151,15 @@ __device__ __forceinline__ uint64_t smem_desc(uint32_t saddr, uint32_t row_bytes
     return d;
 }
 
+// As smem_desc, for a start address anywhere inside a tile that TMA wrote
+// from a 1024-byte aligned base: whole pixel lines (rows) past the base, plus
+// 32-byte K steps within a line. The swizzle pattern is taken from the
+// address bits of each access, as TMA applied it, so the matrix base offset
+// field stays 0.
+__device__ __forceinline__ uint64_t smem_desc_at(uint32_t saddr, uint32_t row_bytes) {
+    return smem_desc(saddr, row_bytes);
+}
+
 // bf16 x bf16 -> f32, both operands K-major, M x N tile.
 __host__ __device__ constexpr uint32_t idesc_bf16(uint32_t m, uint32_t n) {
     return (1u << 4) | (1u << 7) | (1u << 10) | ((n >> 3) << 17) | ((m >> 4) << 24);

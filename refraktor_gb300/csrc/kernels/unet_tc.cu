@@ -56,19 +56,30 @@ struct conv_args {
     int* err;
 };
 
-template <int BK, int BN>
+// COLS (column-tap reuse): a K block covers one tap row dy and all three
+// column taps. Its A box holds 136 pixels of each image row, from x0 - 1 on
+// (130 used, 136 keeps every row 1024-byte aligned for 128-byte swizzle and
+// 512-byte aligned for 64-byte swizzle), and the MMAs of column tap dx read it
+// through a descriptor that starts dx pixel lines later. The input crosses
+// L2 three times per layer instead of nine.
+template <int BK, int BN, bool COLS>
 struct conv_cfg {
     // R image rows per tile (R accumulators of 128 x BN): small-N layers move
     // R times the bytes per pipeline stage, so the stage round trip is shared
     static constexpr int R = BN >= 128 ? 1 : 128 / BN;
-    static constexpr uint32_t A_ROW = 128u * BK * 2u;  // one image row segment
+    static constexpr int A_PIX = COLS ? 136 : 128;               // pixel lines per image row
+    static constexpr uint32_t A_ROW = (uint32_t)A_PIX * BK * 2u;  // one image row segment
     static constexpr uint32_t A_BYTES = R * A_ROW;
-    static constexpr uint32_t B_BYTES = (uint32_t)BN * BK * 2u;
-    static constexpr uint32_t STAGE_BYTES = A_BYTES + B_BYTES;
+    static constexpr int NB = COLS ? 3 : 1;                       // weight tiles per stage
+    static constexpr uint32_t B_TILE = (uint32_t)BN * BK * 2u;
+    static constexpr uint32_t LOAD_BYTES = A_BYTES + NB * B_TILE;  // bytes the TMA writes per stage
+    static constexpr uint32_t STAGE_BYTES = (LOAD_BYTES + 1023u) & ~1023u;
+    static constexpr int TAPS = COLS ? 3 : 9;                     // K blocks per input channel block
     // one persistent CTA per SM: as many stages as fit in ~190 KB, at most 8
     static constexpr int STAGES = (194560u / STAGE_BYTES > 8) ? 8 : (int)(194560u / STAGE_BYTES);
     static constexpr uint32_t SMEM = STAGES * STAGE_BYTES + 1024u;
     static constexpr uint32_t TMEM_COLS = 2u * R * BN;  // two sets of R accumulators
+    static_assert(!COLS || (A_BYTES % 1024u == 0 && B_TILE % 1024u == 0), "COLS tiles must stay 1024-byte aligned");
 };
 
 __device__ __forceinline__ void store_bf16x32(bf16* dst, const float (&v)[32]) {
@@ -127,7 +138,8 @@ __device__ __forceinline__ void load_bf16x16(const bf16* src, float (&v)[16]) {
     }
 }
 
-constexpr int kEpiWarps = 8;  // two warps per TMEM lane quarter, each half of the columns
+constexpr int kEpiWarps = 8;
+constexpr bool kColumnTapReuse = true;  // two warps per TMEM lane quarter, each half of the columns
 
 // Persistent: one CTA per SM walks the tiles (R rows x 128-pixel segment x BN
 // output channels) t = blockIdx.x, blockIdx.x + gridDim.x, ...
@@ -135,10 +147,10 @@ constexpr int kEpiWarps = 8;  // two warps per TMEM lane quarter, each half of t
 // w / 4), warp 8 lane 0: TMA producer over a ring of stages that runs across
 // tiles, warp 9 lane 0: MMA issuer. Two TMEM accumulators: the MMAs of tile
 // i + 1 run while the epilogue drains tile i (acc_full / acc_empty barriers).
-template <int BK, int BN>
+template <int BK, int BN, bool COLS>
 __global__ void __launch_bounds__(320, 1) conv3x3_tc(const __grid_constant__ CUtensorMap tmA,
                                                      const __grid_constant__ CUtensorMap tmB, conv_args p) {
-    using C = conv_cfg<BK, BN>;
+    using C = conv_cfg<BK, BN, COLS>;
     extern __shared__ uint8_t smem_dyn[];
     uint8_t* base = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_dyn) + 1023) & ~(uintptr_t)1023);
     __shared__ uint64_t full[C::STAGES], empty[C::STAGES], acc_full[2], acc_empty[2];
@@ -150,7 +162,7 @@ __global__ void __launch_bounds__(320, 1) conv3x3_tc(const __grid_constant__ CUt
     const int rows_t = (p.h + C::R - 1) / C::R;            // row groups per image
     const int ntiles = p.n_img * rows_t * p.tiles_x * ntn;
     const int kpt = p.cin / BK;                            // K blocks per tap
-    const int nk = 9 * kpt;
+    const int nk = C::TAPS * kpt;
 
     if (warp == 0) tc::tmem_alloc(&tmem_base, C::TMEM_COLS);
     if (threadIdx.x == 32) {
@@ -188,9 +200,19 @@ __global__ void __launch_bounds__(320, 1) conv3x3_tc(const __grid_constant__ CUt
                     }
                     const int tap = kb / kpt, cb = kb - tap * kpt;
                     uint8_t* sa = base + (size_t)s * C::STAGE_BYTES;
-                    tc::mbar_expect_tx(&full[s], C::STAGE_BYTES);
-                    tc::tma_load_4d(sa, &tmA, &full[s], p.cin_off + cb * BK, xt * 128 + tap % 3 - 1, y + tap / 3 - 1, img);
-                    tc::tma_load_2d(sa + C::A_BYTES, &tmB, &full[s], tap * p.cin + cb * BK, n0);
+                    tc::mbar_expect_tx(&full[s], C::LOAD_BYTES);
+                    if (COLS) {
+                        // tap = dy row: pixels x0 - 1 .. x0 + 134, the three column taps' weights
+                        tc::tma_load_4d(sa, &tmA, &full[s], p.cin_off + cb * BK, xt * 128 - 1, y + tap - 1, img);
+#pragma unroll
+                        for (int dx = 0; dx < 3; dx++)
+                            tc::tma_load_2d(sa + C::A_BYTES + dx * C::B_TILE, &tmB, &full[s], (tap * 3 + dx) * p.cin + cb * BK,
+                                            n0);
+                    } else {
+                        tc::tma_load_4d(sa, &tmA, &full[s], p.cin_off + cb * BK, xt * 128 + tap % 3 - 1, y + tap / 3 - 1,
+                                        img);
+                        tc::tma_load_2d(sa + C::A_BYTES, &tmB, &full[s], tap * p.cin + cb * BK, n0);
+                    }
                 }
             }
             if (!ok) {
@@ -225,9 +247,13 @@ __global__ void __launch_bounds__(320, 1) conv3x3_tc(const __grid_constant__ CUt
 #pragma unroll
                     for (int r = 0; r < C::R; r++)
 #pragma unroll
-                        for (int kk = 0; kk < BK / 16; kk++)
-                            tc::mma_bf16(acc + (uint32_t)(r * BN), tc::smem_desc(sa + r * C::A_ROW + kk * 32, BK * 2),
-                                         tc::smem_desc(sb + kk * 32, BK * 2), idesc, (kb | kk) != 0 ? 1u : 0u);
+                        for (int dx = 0; dx < C::NB; dx++)
+#pragma unroll
+                            for (int kk = 0; kk < BK / 16; kk++)
+                                tc::mma_bf16(acc + (uint32_t)(r * BN),
+                                             tc::smem_desc_at(sa + r * C::A_ROW + dx * (BK * 2) + kk * 32, BK * 2),
+                                             tc::smem_desc(sb + dx * C::B_TILE + kk * 32, BK * 2), idesc,
+                                             (kb | dx | kk) != 0 ? 1u : 0u);
                     tc::mma_commit(&empty[s]);
                 }
                 tc::mma_commit(&acc_full[b]);  // also on failure: arrives once the issued MMAs are done
@@ -488,17 +514,17 @@ int sm_count_cached() {
     return n;
 }
 
-template <int BK, int BN>
+template <int BK, int BN, bool COLS>
 cudaError_t launch_conv(const CUtensorMap& a, const CUtensorMap& b, const conv_args& p, cudaStream_t s) {
-    using C = conv_cfg<BK, BN>;
+    using C = conv_cfg<BK, BN, COLS>;
     static std::once_flag once;
     static cudaError_t attr = cudaSuccess;
-    std::call_once(once, [] { attr = raise_smem(conv3x3_tc<BK, BN>, C::SMEM); });
+    std::call_once(once, [] { attr = raise_smem(conv3x3_tc<BK, BN, COLS>, C::SMEM); });
     if (attr != cudaSuccess) return attr;
     const long long tiles = (long long)p.n_img * ((p.h + C::R - 1) / C::R) * p.tiles_x * (p.cout / BN);
     if (tiles > 0x7FFFFFFFLL) return cudaErrorInvalidValue;
     const int grid = (int)std::min<long long>(tiles, sm_count_cached());
-    conv3x3_tc<BK, BN><<<grid, 32 * (kEpiWarps + 2), C::SMEM, s>>>(a, b, p);
+    conv3x3_tc<BK, BN, COLS><<<grid, 32 * (kEpiWarps + 2), C::SMEM, s>>>(a, b, p);
     return cudaGetLastError();
 }
 
@@ -535,14 +561,17 @@ extern "C" cudaError_t rfk_unet_conv3x3(const void* in, int n_img, int h, int w,
         return cudaErrorMisalignedAddress;
     const int bk = (cin % 64 == 0 && in_coff % 64 == 0) ? 64 : 32;
     const int bn = pick_bn(cout);
+    // narrow layers (several image rows per tile) reuse one input tile for
+    // the three column taps
+    const bool cols = kColumnTapReuse && bn <= 64;
     CUtensorMap ma, mb;
     const CUtensorMapSwizzle sw = bk == 64 ? CU_TENSOR_MAP_SWIZZLE_128B : CU_TENSOR_MAP_SWIZZLE_64B;
     {
         cuuint64_t dims[4] = {(cuuint64_t)in_cstride, (cuuint64_t)w, (cuuint64_t)h, (cuuint64_t)n_img};
         cuuint64_t str[3] = {(cuuint64_t)in_cstride * 2, (cuuint64_t)w * in_cstride * 2, (cuuint64_t)h * w * in_cstride * 2};
-        // R image rows per tile, as conv_cfg<BK, BN>::R
+        // R image rows per tile and pixel lines per row, as conv_cfg<BK, BN, COLS>
         const cuuint32_t rows = bn >= 128 ? 1u : (cuuint32_t)(128 / bn);
-        cuuint32_t box[4] = {(cuuint32_t)bk, 128, rows, 1};
+        cuuint32_t box[4] = {(cuuint32_t)bk, cols ? 136u : 128u, rows, 1};
         if (!make_map(&ma, in, 4, dims, str, box, sw)) return cudaErrorInvalidValue;
     }
     {
@@ -572,17 +601,17 @@ extern "C" cudaError_t rfk_unet_conv3x3(const void* in, int n_img, int h, int w,
     p.err = err;
     if (bk == 64) {
         switch (bn) {
-        case 256: return launch_conv<64, 256>(ma, mb, p, s);
-        case 128: return launch_conv<64, 128>(ma, mb, p, s);
-        case 64: return launch_conv<64, 64>(ma, mb, p, s);
-        default: return launch_conv<64, 32>(ma, mb, p, s);
+        case 256: return launch_conv<64, 256, false>(ma, mb, p, s);
+        case 128: return launch_conv<64, 128, false>(ma, mb, p, s);
+        case 64: return cols ? launch_conv<64, 64, true>(ma, mb, p, s) : launch_conv<64, 64, false>(ma, mb, p, s);
+        default: return cols ? launch_conv<64, 32, true>(ma, mb, p, s) : launch_conv<64, 32, false>(ma, mb, p, s);
         }
     }
     switch (bn) {
-    case 256: return launch_conv<32, 256>(ma, mb, p, s);
-    case 128: return launch_conv<32, 128>(ma, mb, p, s);
-    case 64: return launch_conv<32, 64>(ma, mb, p, s);
-    default: return launch_conv<32, 32>(ma, mb, p, s);
+    case 256: return launch_conv<32, 256, false>(ma, mb, p, s);
+    case 128: return launch_conv<32, 128, false>(ma, mb, p, s);
+    case 64: return cols ? launch_conv<32, 64, true>(ma, mb, p, s) : launch_conv<32, 64, false>(ma, mb, p, s);
+    default: return cols ? launch_conv<32, 32, true>(ma, mb, p, s) : launch_conv<32, 32, false>(ma, mb, p, s);
     }
 }
 

@@ -63,7 +63,10 @@ def evaluate(db, net, genomes, w: int, h: int, seed: int = 7) -> dict:
     from refraktor_gb300 import librefrakt as lr
 
     fs = [lr.flame.from_json(db, g) for g in genomes]
-    k = lr.flame_compiler().get_flame_kernel(db, fs[0])
+    # one union kernel for the set (the genomes share their structure), with
+    # the launch shape the autotuner picks on the first flame
+    opts, _ = lr.autotune(db, fs[0], fs[0].pack_samples(4, w, h), (w, h))
+    k = lr.flame_compiler().get_flame_kernel(db, fs[0], **opts)
     tm = lr.tonemapper()
     img = torch.empty((h, w, 4), dtype=torch.float32, device="cuda")
     ref = torch.empty((h, w, 4), dtype=torch.float32, device="cuda")
@@ -137,6 +140,8 @@ def main():
     ap.add_argument("--steps", type=int, default=1500)
     ap.add_argument("--batch", type=int, default=16)
     ap.add_argument("--out", default=str(HERE))
+    ap.add_argument("--eval-only", default=None,
+                    help="evaluate these weights (keeping the training record of the eval file in --out)")
     args = ap.parse_args()
     import torch
 
@@ -147,6 +152,18 @@ def main():
     build.build()
     db = lr.flamedb()
     out = Path(args.out)
+    if args.eval_only:
+        net = dn.denoiser.load(args.eval_only)
+        prev = out / "denoiser_eval.json"
+        training = json.loads(prev.read_text()).get("training") if prev.exists() else None
+        eval_g = dataset(db, args.eval, EVAL_SEED0, 1920, 1080)
+        log("evaluation genomes", len(eval_g))
+        ev = evaluate(db, net, eval_g, 1920, 1080)
+        if training:
+            ev["training"] = training
+        prev.write_text(json.dumps(ev, indent=1))
+        log(json.dumps({k: v for k, v in ev.items() if k != "per_flame"}))
+        return
     t0 = time.perf_counter()
     train_g = dataset(db, args.train, TRAIN_SEED0, 512, 512)
     log("training genomes", len(train_g), f"{time.perf_counter() - t0:.1f}s")

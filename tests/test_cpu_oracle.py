@@ -102,6 +102,36 @@ def test_render_single_fixed_point():
     np.testing.assert_allclose(hist[32, 32, :3], [5000, 0, 0])
 
 
+def two_point_chaos_flame() -> dict:
+    """Two near-constant maps (to x = -0.25 and x = +0.25; a zero matrix has
+    no polar form) with weights 0.9 / 0.1
+    and chaos rows that forbid repeating an xform: a chain alternates
+    between the two points, so they get equal counts (0.9 / 0.1 without the
+    chaos rows)."""
+    g = syn.plain_flame(0)
+    g["xforms"] = [{"weight": wt, "color": col, "color_speed": 1.0, "opacity": 1.0,
+                    "vchain": [{"transform": [1e-6, 0, 0, 1e-6, tx, 0], "mod_x": 0, "mod_y": 0, "mod_scale": 1,
+                                "mod_rotate": 0, "variations": {"linear": 1.0}}]}
+                   for wt, col, tx in ((0.9, 0.0, -0.25), (0.1, 1.0, 0.25))]
+    g["chaos"] = [[0.0, 1.0], [1.0, 0.0]]
+    g["palette"] = [[0.0, 1.0, 1.0]] * 256
+    return g
+
+
+def test_render_chaos_rows_alternate():
+    """Chaos (xaos) rows weight the next pick by the previous xform
+    (flame.tpl:170-177): with rows [[0, 1], [1, 0]] every chain alternates."""
+    g = two_point_chaos_flame()
+    hist, draws = orc.render(g, 64, 64, chains=100, passes=50, warmup=60, threads=2, jitter=np.zeros((1, 2)))
+    assert draws == 100 * 50
+    left, right = hist[:, :32, 3].sum(), hist[:, 32:, 3].sum()
+    assert left == right == 2500
+    assert np.count_nonzero(hist[..., 3]) == 2
+    del g["chaos"]
+    hist, _ = orc.render(g, 64, 64, chains=100, passes=50, warmup=60, threads=2, jitter=np.zeros((1, 2)))
+    assert abs(hist[:, :32, 3].sum() - 4500) < 200
+
+
 def test_apply_known_points():
     g = syn.plain_flame(0)
     g["xforms"] = [{"weight": 1.0, "color": 0.25, "color_speed": 0.5, "opacity": 0.7,

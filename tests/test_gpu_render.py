@@ -12,6 +12,7 @@ torch = pytest.importorskip("torch")
 from oracle import oracle as orc
 from refraktor_gb300 import librefrakt as lr
 from refraktor_gb300 import synthetic as syn
+from tests.pick_tables import alias_distribution
 
 pytestmark = pytest.mark.gpu
 
@@ -298,6 +299,69 @@ def test_hd_render_colour_matches_oracle(db, comp):
         assert d < 1.25 * floor, (c, d, floor)
 
 
+def test_pick_tables_encode_xform_weights(db, comp):
+    """The alias tables of a prepared block pick xform k with probability
+    weight_k / sum (zero weights never), and chaos row r with probability
+    chaos[r][k] * weight_k / sum over k (flame.tpl:110-123, :170-177)."""
+    g = syn.hd_flame(5)
+    n = len(g["xforms"])
+    g["xforms"][2]["weight"] = 0.0
+    rng = np.random.default_rng(9)
+    chaos = rng.uniform(0, 2, size=(n, n)) * (rng.uniform(size=(n, n)) < 0.7)
+    chaos[3] = 0.0  # an all-zero row picks xform 0, as the reference's fallback
+    g["chaos"] = chaos.tolist()
+    f = lr.flame.from_json(db, g)
+    k = comp.get_flame_kernel(db, f)
+    got = k.prepare_samples(f.pack_samples(4, 320, 240), [0], [0.0])[0]
+    R = f.size_reals()
+    wt = np.array([x["weight"] for x in g["xforms"]], dtype=np.float64)
+    p = alias_distribution(got, R, n)
+    np.testing.assert_allclose(p, wt / wt.sum(), atol=2e-6)
+    assert p[2] == 0.0
+    for r in range(n):
+        row = chaos[r] * wt
+        want = row / row.sum() if row.sum() > 0 else np.eye(n)[0]
+        pr = alias_distribution(got, R, n, row=r)
+        np.testing.assert_allclose(pr, want, atol=2e-6, err_msg=str(r))
+        assert np.all(pr[row == 0] == 0.0) or row.sum() == 0
+
+
+@pytest.mark.parametrize("sort", [2, 1, -1])
+def test_chaos_rows_alternate(db, comp, sort):
+    """Chaos rows [[0, 1], [1, 0]] on two near-constant maps (weights 0.9 /
+    0.1): every chain alternates between the two points, so under a pass cap
+    of an even number of passes both get exactly half of the draws, as in the
+    oracle (tests/test_cpu_oracle.py)."""
+    from tests.test_cpu_oracle import two_point_chaos_flame
+
+    g = two_point_chaos_flame()
+    f = lr.flame.from_json(db, g)
+    k = comp.get_flame_kernel(db, f, sort=sort)
+    assert k.info["chaos"] == 1
+    st = k.warmup(f.pack_samples(4, 64, 64), (64, 64), seed=3, count=20)
+    r = k.bin(st, lr.bailout_args(iters=20, millis=0, quality=0))
+    d = st.bins().cpu().numpy()[..., 3].astype(np.float64)
+    assert r.draw_count == r.total_passes and d.sum() == r.draw_count
+    assert d[:, :32].sum() == d[:, 32:].sum() == r.draw_count / 2
+
+
+def test_chaos_render_matches_oracle(db, comp):
+    """A chaos flame (8 xforms + final, random chaos rows with zeros) against
+    the FP64 oracle below the Monte-Carlo noise floor, density and colour."""
+    # a seed whose chaos flame covers a third of the 160 x 90 frame (many
+    # seeds collapse onto a few pixels, where FP32 pixel rounding outweighs
+    # the Monte-Carlo noise)
+    g = syn.hd_flame(21)
+    rng = np.random.default_rng(121)
+    n = len(g["xforms"])
+    rows = rng.uniform(0.2, 1.5, size=(n, n)) * (rng.uniform(size=(n, n)) < 0.75)
+    rows[np.arange(n), rng.integers(0, n, n)] += 0.5  # no all-zero row
+    g["chaos"] = rows.tolist()
+    res = _render_parity(db, comp, g, 160, 90, (64.0,), channels=(0, 1, 2, 3))
+    for (spp, c), (d, floor) in res.items():
+        assert d < 1.25 * floor, (c, d, floor)
+
+
 @pytest.mark.parametrize("sort,flush", [(2, 0), (2, 1), (2, 2), (2, 3), (1, 2), (-1, 1)])
 def test_sort_and_flush_variants_agree(db, comp, sort, flush):
     """Every (sort, flush) variant the autotuner may pick renders the same
@@ -389,7 +453,12 @@ def test_temporal_multiplier_spreads_samples_over_the_segment(db, comp):
     want = k.prepare_samples(samples, seg, t, seed=9).astype(np.float64)
     assert got.shape == want.shape
     pal0 = k.info["sample_floats"] - 1024
-    idx = np.r_[0:4, 6:pal0]
+    R, nx = keys[0].size_reals(), k.info["num_xforms"]
+    idx = np.r_[0:4, 6:R]
     ulp = np.spacing(np.maximum(np.abs(got), np.abs(want)).astype(np.float32)).astype(np.float64)
     assert np.all(np.abs(got - want)[:, idx] <= 4 * ulp[:, idx])
     assert np.all(np.abs(got - want)[:, pal0:] <= 1.0 / 255 + 1e-6)
+    # weights a few ulps apart may give alias tables of another shape that
+    # encode the same pick distribution
+    for i in range(S):
+        np.testing.assert_allclose(alias_distribution(got[i], R, nx), alias_distribution(want[i], R, nx), atol=1e-5)
