@@ -234,6 +234,26 @@ extern "C" __global__ void __launch_bounds__(256) rfk_prepare(const float4* __re
     for (unsigned i = threadIdx.x; i < RFK_SAMPLE_FLOATS; i += blockDim.x) dst[i] = P[i];
 }
 
+// ------------------------------------------------------- parameter block --
+// 8-bit RGB of a palette entry (the prepared palette holds k / 255).
+__device__ __forceinline__ unsigned rfk_rgb8(float4 c) {
+    return (unsigned)__float2int_rn(c.x * 255.0f) | ((unsigned)__float2int_rn(c.y * 255.0f) << 8) |
+           ((unsigned)__float2int_rn(c.z * 255.0f) << 16);
+}
+
+// All threads of the block: copies a prepared parameter block into shared
+// memory P. The palette goes in as 8-bit RGB pairs (entry i, entry i + 1) in
+// the first half of its float4 region, as the reference keeps it (uchar3,
+// refactor.cu:128-140): a draw reads both ends of its colour interval with one
+// 8-byte load from a 2 KB table instead of two 16-byte loads from 4 KB, which
+// cuts the shared-memory wavefronts of the random palette reads.
+__device__ __forceinline__ void rfk_load_params(float* P, const float* __restrict__ src) {
+    for (unsigned i = threadIdx.x; i < RFK_OFF_PAL; i += RFK_BLOCK) P[i] = src[i];
+    uint2* pal = reinterpret_cast<uint2*>(P + RFK_OFF_PAL);
+    const float4* sp = reinterpret_cast<const float4*>(src + RFK_OFF_PAL);
+    for (unsigned i = threadIdx.x; i < 256; i += RFK_BLOCK) pal[i] = make_uint2(rfk_rgb8(sp[i]), rfk_rgb8(sp[min(i + 1, 255u)]));
+}
+
 // ------------------------------------------------------------- chain step --
 // Xform pick from a uniform u in [0, 1) through the alias table (of the
 // previous xform's chaos row when there is one).
@@ -274,15 +294,17 @@ __device__ __forceinline__ int rfk_move(int k, float& x, float& y, float& c, Rng
     sy = truncf(sy);
     hit = 0;
     if (sx >= 0.0f && sy >= 0.0f && sx < (float)w && sy < (float)h && op > 0.0f) {
+        // lerp between the 8-bit entries at floor and floor + 1 of colour *
+        // 255 (at an integer the weight of floor + 1 is 0, as the reference's
+        // ceil), / 255, * opacity (refactor.cu:366-378)
         const float pi = fminf(fmaxf(col, 0.0f), 1.0f) * 255.0f;
         const float lo_f = floorf(pi);
-        const int lo = (int)lo_f, hi = (int)ceilf(pi);
         const float mix = pi - lo_f;
-        const float4* pal = reinterpret_cast<const float4*>(P + RFK_OFF_PAL);
-        const float4 a = pal[lo], b = pal[hi];
-        contrib.x = ((1.0f - mix) * a.x + mix * b.x) * op;
-        contrib.y = ((1.0f - mix) * a.y + mix * b.y) * op;
-        contrib.z = ((1.0f - mix) * a.z + mix * b.z) * op;
+        const uint2 e = reinterpret_cast<const uint2*>(P + RFK_OFF_PAL)[(int)lo_f];
+        const float s = op * (1.0f / 255.0f);
+        contrib.x = ((1.0f - mix) * (float)(e.x & 0xFFu) + mix * (float)(e.y & 0xFFu)) * s;
+        contrib.y = ((1.0f - mix) * (float)((e.x >> 8) & 0xFFu) + mix * (float)((e.y >> 8) & 0xFFu)) * s;
+        contrib.z = ((1.0f - mix) * (float)((e.x >> 16) & 0xFFu) + mix * (float)((e.y >> 16) & 0xFFu)) * s;
         contrib.w = op;
         hit = (unsigned)(255.0f * op);
         return (int)sy * (int)w + (int)sx;
@@ -349,14 +371,15 @@ __device__ __forceinline__ void rfk_sort_chains(float4* __restrict__ region, con
 // Block-wide counting sort of the block's RFK_BLOCK * RFK_CPT chains by picked
 // xform (deterministic order: xform-major, then warp, then round, then lane),
 // in place in the chain array: every thread has read its own slots (values v,
-// picks k) before the call, and the scatter comes after two barriers.
-// counts[RFK_NX * RFK_NW] must be zero on entry; it is used in place for the
-// starts. `next` (the other counter set) is cleared between the first and the
-// second barrier: every thread finished the previous pass's reads of it before
-// the first barrier, and every thread's next-pass updates of it come after the
-// second. Afterwards slot q * RFK_BLOCK + t holds thread t's round-q chain, so
-// a warp's round covers 32 consecutive slots of one xform run except at run
-// ends.
+// picks k) before the call, and the scatter comes after a barrier. Two
+// barriers per pass: after the first, every warp derives the starts it needs
+// from the per-(xform, warp) counters itself (no single-warp scan and second
+// barrier). counts[RFK_NX * RFK_NW] must be zero on entry. `next` (the other
+// counter set) is cleared after the first barrier: every warp read it in the
+// previous pass before that pass's second barrier, and its next-pass updates
+// come after this pass's second barrier. Afterwards slot q * RFK_BLOCK + t
+// holds thread t's round-q chain, so a warp's round covers 32 consecutive
+// slots of one xform run except at run ends.
 __device__ __forceinline__ void rfk_block_sort(float4* __restrict__ chains, const float4 (&v)[RFK_CPT],
                                                const int (&k)[RFK_CPT], unsigned* __restrict__ counts,
                                                unsigned* __restrict__ next) {
@@ -373,36 +396,28 @@ __device__ __forceinline__ void rfk_block_sort(float4* __restrict__ chains, cons
     }
     __syncthreads();
     for (unsigned i = threadIdx.x; i < RFK_NX * RFK_NW; i += RFK_BLOCK) next[i] = 0u;
-    if (warp == 0) {
-        // exclusive scan of counts[] (xform-major) by one warp
-        constexpr unsigned N = RFK_NX * RFK_NW;
-        constexpr unsigned E = (N + 31) / 32;
-        unsigned local[E];
-        unsigned sum = 0;
+    // lane x < RFK_NX: the block's count of xform x and the part of it in
+    // warps before this one; an exclusive scan of the counts over lanes gives
+    // the start of xform x's run, and start + part this warp's start in it
+    unsigned tot = 0, part = 0;
+    if (lane < RFK_NX) {
 #pragma unroll
-        for (unsigned e = 0; e < E; e++) {
-            const unsigned i = lane * E + e;
-            local[e] = (i < N) ? counts[i] : 0u;
-            sum += local[e];
-        }
-        unsigned incl = sum;
-#pragma unroll
-        for (int d = 1; d < 32; d <<= 1) {
-            const unsigned u = __shfl_up_sync(0xffffffffu, incl, d);
-            if ((int)lane >= d) incl += u;
-        }
-        unsigned run = incl - sum;
-#pragma unroll
-        for (unsigned e = 0; e < E; e++) {
-            const unsigned i = lane * E + e;
-            if (i < N) counts[i] = run;
-            run += local[e];
+        for (unsigned w = 0; w < RFK_NW; w++) {
+            const unsigned c = counts[lane * RFK_NW + w];
+            tot += c;
+            part += (w < warp) ? c : 0u;
         }
     }
-    __syncthreads();
+    unsigned incl = tot;
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+        const unsigned u = __shfl_up_sync(0xffffffffu, incl, d);
+        if ((int)lane >= d) incl += u;
+    }
+    const unsigned start = incl - tot + part;
 #pragma unroll
     for (int q = 0; q < RFK_CPT; q++) {
-        const unsigned pos = counts[k[q] * RFK_NW + warp] + off[q];
+        const unsigned pos = __shfl_sync(0xffffffffu, start, k[q]) + off[q];
         chains[pos] = make_float4(v[q].x, v[q].y, v[q].z, __int_as_float(k[q]));
     }
     __syncthreads();
@@ -709,7 +724,7 @@ extern "C" __global__ void RFK_BIN_BOUNDS rfk_bin(rfk_bin_args a) {
     rfk_pass_smem_init(sm);
     const unsigned lane_stream = blockIdx.x * RFK_BLOCK + threadIdx.x;
     const float* src = a.samples + (size_t)blockIdx.x * RFK_SAMPLE_FLOATS;
-    for (unsigned i = threadIdx.x; i < RFK_SAMPLE_FLOATS; i += RFK_BLOCK) P[i] = src[i];
+    rfk_load_params(P, src);
     if (threadIdx.x == 0) {
         s_hits = 0;
         s_draws = 0;
@@ -779,7 +794,7 @@ extern "C" __global__ void RFK_BIN_BOUNDS rfk_warmup(const float* __restrict__ s
     __shared__ rfk_pass_smem sm;
     rfk_pass_smem_init(sm);
     const float* src = samples + (size_t)blockIdx.x * RFK_SAMPLE_FLOATS;
-    for (unsigned i = threadIdx.x; i < RFK_SAMPLE_FLOATS; i += RFK_BLOCK) P[i] = src[i];
+    rfk_load_params(P, src);
     __syncthreads();
     const unsigned total = gridDim.x * RFK_BLOCK * RFK_CPT;
     const unsigned lane_stream = blockIdx.x * RFK_BLOCK + threadIdx.x;
@@ -848,7 +863,7 @@ extern "C" __global__ void RFK_BIN_BOUNDS rfk_bin_tm(rfk_bin_args a) {
     unsigned smp = blockIdx.x;
     // chain of slot q of temporal sample smp: smp * RFK_BLOCK + t + q * cstride
     const unsigned cstride = S * RFK_BLOCK;
-    for (unsigned i = threadIdx.x; i < RFK_SAMPLE_FLOATS; i += RFK_BLOCK) P[i] = a.samples[(size_t)smp * RFK_SAMPLE_FLOATS + i];
+    rfk_load_params(P, a.samples + (size_t)smp * RFK_SAMPLE_FLOATS);
     rfk_load_chains(sm, a.st, smp * RFK_BLOCK + threadIdx.x, cstride);
     __syncthreads();
 
@@ -907,8 +922,7 @@ extern "C" __global__ void RFK_BIN_BOUNDS rfk_bin_tm(rfk_bin_args a) {
             rfk_store_chains(sm, a.st, smp * RFK_BLOCK + threadIdx.x, cstride);
             cur = nxt;
             smp = blockIdx.x + gridDim.x * (unsigned)cur;
-            for (unsigned i = threadIdx.x; i < RFK_SAMPLE_FLOATS; i += RFK_BLOCK)
-                P[i] = a.samples[(size_t)smp * RFK_SAMPLE_FLOATS + i];
+            rfk_load_params(P, a.samples + (size_t)smp * RFK_SAMPLE_FLOATS);
             rfk_load_chains(sm, a.st, smp * RFK_BLOCK + threadIdx.x, cstride);
             in_slice = 0;
             __syncthreads();
@@ -1036,7 +1050,7 @@ extern "C" __global__ void RFK_BIN_BOUNDS rfk_bin_batch(rfk_batch_args a) {
         if (u < 0) break;
         const unsigned long long item = s_item;
         const rfk_unit U = a.units[u];
-        for (unsigned i = threadIdx.x; i < RFK_SAMPLE_FLOATS; i += RFK_BLOCK) P[i] = U.params[i];
+        rfk_load_params(P, U.params);
         __syncthreads();
         if (threadIdx.x == 0) rfk_batch_jitter(P, U.params, item, call_id, pass, a.seed, a.salt);
         __syncthreads();
