@@ -13,6 +13,15 @@ the repository. Flags follow the reference's host code:
                     (src/librefrakt/src/flame_compiler.cpp:773-780)
 Each module is written as <name>.cubin with <name>.json holding the lowered
 kernel names.
+
+The reference's chaos-game module (refactor.cu) is specialised per flame: for
+each flame of REF_FLAMES its flame_generated.h is produced by
+oracle/ref_flame.py (flame.tpl + the flang rule table) and the module is
+compiled with the reference's options (flame_compiler.cpp:600-620, :834-860:
+-extra-device-vectorization, -default-device, -lineinfo, -use_fast_math,
+NUM_SHUF_BUFS 512 and the launch-shape defines, refrakt/random.h and
+refrakt/flamelib.h as headers) into refactor_<flame>.cubin; its json also
+holds the genome, the launch shape and the flame's real count.
 """
 from __future__ import annotations
 
@@ -42,10 +51,15 @@ def _nvrtc() -> C.CDLL:
     return L
 
 
-def compile_module(src: str, name: str, kernels: list[str], flags: list[str], arch: str = "sm_103a") -> tuple[bytes, dict]:
+def compile_module(src: str, name: str, kernels: list[str], flags: list[str], arch: str = "sm_103a",
+                   headers: dict[str, str] | None = None) -> tuple[bytes, dict]:
     L = _nvrtc()
     prog = C.c_void_p()
-    r = L.nvrtcCreateProgram(C.byref(prog), src.encode(), f"{name}.cu".encode(), 0, None, None)
+    headers = headers or {}
+    hsrc = (C.c_char_p * max(1, len(headers)))(*[v.encode() for v in headers.values()])
+    hname = (C.c_char_p * max(1, len(headers)))(*[k.encode() for k in headers])
+    r = L.nvrtcCreateProgram(C.byref(prog), src.encode(), f"{name}.cu".encode(), len(headers),
+                             hsrc if headers else None, hname if headers else None)
     if r:
         raise RuntimeError(f"nvrtcCreateProgram: {L.nvrtcGetErrorString(r).decode()}")
     for k in kernels:
@@ -71,6 +85,50 @@ def compile_module(src: str, name: str, kernels: list[str], flags: list[str], ar
     return buf.raw, lowered
 
 
+# Flames whose reference chaos-game module is built: genome maker (seeded),
+# image size, threads per block and blocks per SM (the grid is blocks per SM
+# x the 152 SMs of a GB300, fixed at compile time through TOTAL_THREADS).
+def _ref_flames() -> dict:
+    sys.path.insert(0, str(HERE.parent))
+    from refraktor_gb300 import synthetic as syn
+
+    return {
+        "c0": (syn.plain_flame(0), 512, 512, 128, 8),
+        "hd": (syn.hd_flame(21), 320, 180, 128, 8),
+    }
+
+
+REF_SMS = 152
+
+
+def build_flames(ref_root: Path) -> None:
+    from oracle import oracle as orc
+    from oracle import ref_flame
+
+    rel = "assets/kernels/refactor.cu"
+    inc = Path(ref_root) / "assets" / "kernels" / "include" / "refrakt"
+    for tag, (g, w, h, tpb, bpmp) in _ref_flames().items():
+        R = orc.size_reals(g)
+        header = ref_flame.flame_header(Path(ref_root), g, orc.affine_indices(g))
+        grid = bpmp * REF_SMS
+        flags = ["-extra-device-vectorization", "-default-device", "-lineinfo", "-use_fast_math",
+                 "-DNUM_SHUF_BUFS=512", f"-DTHREADS_PER_BLOCK={tpb}", f"-DBLOCKS_PER_MP={bpmp}",
+                 f"-DFLAME_SIZE_REALS={R}", f"-DFLAME_SIZE_BYTES={4 * R}", f"-DTOTAL_THREADS={grid * tpb}",
+                 "-DFLAMEDB_HASH=rfkharness"]
+        if "chaos" in g:
+            flags.append("-DUSE_CHAOS")
+        headers = {"flame_generated.h": header, "refrakt/random.h": (inc / "random.h").read_text(),
+                   "refrakt/flamelib.h": (inc / "flamelib.h").read_text()}
+        names = ["warmup", "bin", "get_sample_state_size", "shuf_bufs"]
+        cubin, lowered = compile_module((Path(ref_root) / rel).read_text(), f"refactor_{tag}", names, flags,
+                                        headers=headers)
+        (OUT / f"refactor_{tag}.cubin").write_bytes(cubin)
+        (OUT / f"refactor_{tag}.json").write_text(json.dumps(
+            {"source": rel, "kernels": lowered, "flags": flags, "genome": g, "width": w, "height": h,
+             "threads_per_block": tpb, "blocks_per_sm": bpmp, "grid": grid, "size_reals": R,
+             "num_shuf_bufs": 512}, indent=1))
+
+
 def build(ref_root: Path) -> None:
     OUT.mkdir(exist_ok=True)
     for name, (rel, kernels, flags) in MODULES.items():
@@ -78,6 +136,7 @@ def build(ref_root: Path) -> None:
         cubin, lowered = compile_module(src_path.read_text(), name, kernels, flags)
         (OUT / f"{name}.cubin").write_bytes(cubin)
         (OUT / f"{name}.json").write_text(json.dumps({"source": rel, "kernels": lowered, "flags": flags}, indent=1))
+    build_flames(ref_root)
     print(f"reference kernels built into {OUT}")
 
 

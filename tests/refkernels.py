@@ -36,20 +36,39 @@ def _check(r: int, what: str) -> None:
         raise RuntimeError(f"{what}: {_rt().cudaGetErrorString(r).decode()}")
 
 
+def meta(module: str) -> dict:
+    return json.loads((REF / f"{module}.json").read_text())
+
+
+def _library(module: str) -> C.c_void_p:
+    key = ("lib", module)
+    if key not in _libs:
+        data = (REF / f"{module}.cubin").read_bytes()
+        buf = C.create_string_buffer(data, len(data))
+        lib = C.c_void_p()
+        _check(_rt().cudaLibraryLoadData(C.byref(lib), buf, None, None, 0, None, None, 0), "cudaLibraryLoadData")
+        _libs[key] = lib
+        _libs[("buf", module)] = buf
+    return _libs[key]
+
+
 def kernel(module: str, name: str) -> C.c_void_p:
     key = (module, name)
     if key in _libs:
         return _libs[key]
-    meta = json.loads((REF / f"{module}.json").read_text())
-    data = (REF / f"{module}.cubin").read_bytes()
-    buf = C.create_string_buffer(data, len(data))
-    lib = C.c_void_p()
-    _check(_rt().cudaLibraryLoadData(C.byref(lib), buf, None, None, 0, None, None, 0), "cudaLibraryLoadData")
     k = C.c_void_p()
-    _check(_rt().cudaLibraryGetKernel(C.byref(k), lib, meta["kernels"][name].encode()), "cudaLibraryGetKernel")
+    _check(_rt().cudaLibraryGetKernel(C.byref(k), _library(module), meta(module)["kernels"][name].encode()),
+           "cudaLibraryGetKernel")
     _libs[key] = k
-    _libs[("buf",) + key] = (buf, lib)
     return k
+
+
+def global_symbol(module: str, name: str) -> tuple[int, int]:
+    """Device address and size in bytes of a __device__ variable of a module."""
+    ptr, size = C.c_void_p(), C.c_size_t(0)
+    _check(_rt().cudaLibraryGetGlobal(C.byref(ptr), C.byref(size), _library(module), meta(module)["kernels"][name].encode()),
+           "cudaLibraryGetGlobal")
+    return int(ptr.value), int(size.value)
 
 
 class Dim3(C.Structure):
