@@ -21,7 +21,13 @@ compiled with the reference's options (flame_compiler.cpp:600-620, :834-860:
 -extra-device-vectorization, -default-device, -lineinfo, -use_fast_math,
 NUM_SHUF_BUFS 512 and the launch-shape defines, refrakt/random.h and
 refrakt/flamelib.h as headers) into refactor_<flame>.cubin; its json also
-holds the genome, the launch shape and the flame's real count.
+holds the genome, the launch shape and the flame's real count. A second
+module, refactor_<flame>_atomic, differs in one place: the histogram update
+of pass_and_draw (refactor.cu:374-381), a non-atomic load / add / store that
+loses the draws of lanes and blocks hitting the same pixel at once, becomes
+four atomic adds of the same contribution (ATOMIC_DRAW below), so that the
+reference's sampling (warp vote, iterator shuffle, xoroshiro64) can be
+compared with librfk's apart from the lost draws.
 """
 from __future__ import annotations
 
@@ -100,6 +106,19 @@ def _ref_flames() -> dict:
 
 REF_SMS = 152
 
+# refactor.cu:374 and :381, and their replacements in the atomic variant
+ATOMIC_DRAW = [("float4 new_bin = bin;", "float4 new_bin = make_float4(0.0f, 0.0f, 0.0f, 0.0f);"),
+               ("bin = new_bin;", "atomicAdd(&bin.x, new_bin.x); atomicAdd(&bin.y, new_bin.y); "
+                                  "atomicAdd(&bin.z, new_bin.z); atomicAdd(&bin.w, new_bin.w);")]
+
+
+def _atomic_draw(src: str) -> str:
+    for old, new in ATOMIC_DRAW:
+        if src.count(old) != 1:
+            raise RuntimeError(f"refactor.cu: expected one '{old}'")
+        src = src.replace(old, new)
+    return src
+
 
 def build_flames(ref_root: Path) -> None:
     from oracle import oracle as orc
@@ -120,13 +139,14 @@ def build_flames(ref_root: Path) -> None:
         headers = {"flame_generated.h": header, "refrakt/random.h": (inc / "random.h").read_text(),
                    "refrakt/flamelib.h": (inc / "flamelib.h").read_text()}
         names = ["warmup", "bin", "get_sample_state_size", "shuf_bufs"]
-        cubin, lowered = compile_module((Path(ref_root) / rel).read_text(), f"refactor_{tag}", names, flags,
-                                        headers=headers)
-        (OUT / f"refactor_{tag}.cubin").write_bytes(cubin)
-        (OUT / f"refactor_{tag}.json").write_text(json.dumps(
-            {"source": rel, "kernels": lowered, "flags": flags, "genome": g, "width": w, "height": h,
-             "threads_per_block": tpb, "blocks_per_sm": bpmp, "grid": grid, "size_reals": R,
-             "num_shuf_bufs": 512}, indent=1))
+        src = (Path(ref_root) / rel).read_text()
+        for suffix, text in (("", src), ("_atomic", _atomic_draw(src))):
+            cubin, lowered = compile_module(text, f"refactor_{tag}{suffix}", names, flags, headers=headers)
+            (OUT / f"refactor_{tag}{suffix}.cubin").write_bytes(cubin)
+            (OUT / f"refactor_{tag}{suffix}.json").write_text(json.dumps(
+                {"source": rel, "atomic_draw": bool(suffix), "kernels": lowered, "flags": flags, "genome": g,
+                 "width": w, "height": h, "threads_per_block": tpb, "blocks_per_sm": bpmp, "grid": grid,
+                 "size_reals": R, "num_shuf_bufs": 512}, indent=1))
 
 
 def build(ref_root: Path) -> None:
