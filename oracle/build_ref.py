@@ -98,9 +98,11 @@ def _ref_flames() -> dict:
     sys.path.insert(0, str(HERE.parent))
     from refraktor_gb300 import synthetic as syn
 
+    bench = json.loads((HERE.parent / "refraktor_gb300" / "workloads" / "hd_1080p.json").read_text())
     return {
         "c0": (syn.plain_flame(0), 512, 512, 128, 8),
         "hd": (syn.hd_flame(21), 320, 180, 128, 8),
+        "bench": (bench, 1920, 1080, 128, 8),
     }
 
 

@@ -28,6 +28,7 @@ from tests import refkernels
 pytestmark = pytest.mark.gpu
 
 WARMUP = 20
+TIMING = None  # (start, end) CUDA events around the bin launch, set by tests/time_reference_kernel.py
 
 
 def _ptr(t) -> C.c_void_p:
@@ -80,10 +81,15 @@ def reference_render(mod: str, seed: int, spp: float) -> tuple[np.ndarray, dict]
     target = int(spp * w * h * 255.0)
     time_ns = 5_000_000_000
     cp = counters.data_ptr()
+    if TIMING:
+        TIMING[0].record()
     refkernels.launch(refkernels.kernel(mod, "bin"), grid, tpb,
                       [_ptr(state), C.c_uint64(target), C.c_uint(0xFFFFFFFF), C.c_uint64(time_ns), _ptr(bins),
                        C.c_uint(w), C.c_uint(h), C.c_void_p(cp), C.c_void_p(cp + 8), _ptr(stop), C.c_int(1),
                        C.c_int(100), _ptr(warm_hits), C.c_void_p(cp + 24), C.c_void_p(cp + 32), _ptr(indices)])
+    if TIMING:
+        TIMING[1].record()
+        torch.cuda.synchronize()
     c = counters.cpu().numpy()
     out = bins.cpu().numpy().astype(np.float64)
     return out, {"quality": c[0] / (w * h * 255.0), "passes": int(c[1]), "draws": c[0] / 255.0,
