@@ -2,18 +2,19 @@
 // zero padding 1) of bf16 NHWC activations as implicit GEMMs on tcgen05, with
 // f32 accumulators in TMEM.
 //
-// conv3x3_tc (forward and input-gradient): one CTA computes a tile of 128
-// output pixels (one row segment of one image) x BN output channels.
+// conv3x3_tc (forward and input-gradient): persistent CTAs walk tiles of R
+// image rows x 128 output pixels x BN output channels.
 //   D[p, n] = sum over taps t and input channels c of A[p + t, c] * W[n, t, c]
-// The K loop runs over (tap, channel block of BK): the A tile of a K block is
-// a TMA box (BK channels x 128 pixels) of the input tensor at the tap's
-// spatial offset - the padding comes from TMA's zero fill outside the image -
-// and the B tile a box (BK x BN) of the weights [cout][9][cin]. Warp 0 (one
-// lane) issues the TMA loads into a ring of shared-memory stages, warp 1 (one
-// lane) issues tcgen05.mma (M 128, N BN, K 16 per instruction) and frees each
-// stage with tcgen05.commit; all four warps then read the accumulator rows
-// from TMEM (warp w owns lanes 32w..32w+31) and apply the epilogue: bias,
-// ReLU, a ReLU-derivative mask, accumulation into the output, bf16 store.
+// The K loop runs over input channel blocks of BK and, depending on MODE
+// (conv_cfg), over taps, tap rows or neither: the A tile of a K block is a
+// TMA box of the NHWC input at the tile's offset - the padding comes from
+// TMA's zero fill outside the image - and the B tiles boxes (BK x BN) of the
+// weights [cout][9][cin]. A producer warp (one lane) issues the TMA loads into
+// a ring of shared-memory stages, an MMA warp (one lane) issues tcgen05.mma
+// (M 128, N BN, K 16 per instruction) and frees each stage with
+// tcgen05.commit; eight epilogue warps read the accumulator rows from TMEM
+// (two per lane quarter) and apply the epilogue: bias, ReLU, a
+// ReLU-derivative mask, accumulation into the output, bf16 or f32 store.
 // The input gradient of a conv is the same kernel on the output gradient with
 // the weights transposed and the taps flipped ([cin][9][cout]).
 //
@@ -56,57 +57,40 @@ struct conv_args {
     int* err;
 };
 
-// COLS (column-tap reuse): a K block covers one tap row dy and all three
-// column taps. Its A box holds 136 pixels of each image row, from x0 - 1 on
-// (130 used, 136 keeps every row 1024-byte aligned for 128-byte swizzle and
-// 512-byte aligned for 64-byte swizzle), and the MMAs of column tap dx read it
-// through a descriptor that starts dx pixel lines later. The input crosses
-// L2 three times per layer instead of nine.
-template <int BK, int BN, bool COLS>
+// Tap reuse. MODE 0: one K block per (tap, input channel block), its A box
+// the 128 pixels of each tile row shifted by the tap. MODE 1 (column taps): a
+// K block covers one tap row dy and the three column taps; its A box holds
+// 136 pixels of each image row from x0 - 1 on (130 used; 136 keeps every row
+// 1024-byte aligned for 128-byte swizzle and 512-byte aligned for 64-byte
+// swizzle) and the MMAs of column tap dx read it through a descriptor that
+// starts dx pixel lines later. MODE 2 (all taps): a K block covers all nine
+// taps of one input channel block; its A box holds the tile's R rows plus the
+// row above and below (R + 2 rows of 136 pixels) and the MMAs of tap (dy, dx)
+// start at row r + dy, pixel line dx. The input crosses L2 nine, three or
+// (R + 2) / R times per layer.
+template <int BK, int BN, int MODE>
 struct conv_cfg {
     // R image rows per tile (R accumulators of 128 x BN): small-N layers move
     // R times the bytes per pipeline stage, so the stage round trip is shared
     static constexpr int R = BN >= 128 ? 1 : 128 / BN;
-    static constexpr int A_PIX = COLS ? 136 : 128;               // pixel lines per image row
-    static constexpr uint32_t A_ROW = (uint32_t)A_PIX * BK * 2u;  // one image row segment
-    static constexpr uint32_t A_BYTES = R * A_ROW;
-    static constexpr int NB = COLS ? 3 : 1;                       // weight tiles per stage
+    static constexpr int A_PIX = MODE ? 136 : 128;                // pixel lines per image row
+    static constexpr int A_ROWS = MODE == 2 ? R + 2 : R;           // image rows per A box
+    static constexpr uint32_t A_ROW = (uint32_t)A_PIX * BK * 2u;   // one image row segment
+    static constexpr uint32_t A_BYTES = A_ROWS * A_ROW;
+    static constexpr int NB = MODE == 2 ? 9 : (MODE == 1 ? 3 : 1);  // weight tiles per stage
     static constexpr uint32_t B_TILE = (uint32_t)BN * BK * 2u;
     static constexpr uint32_t LOAD_BYTES = A_BYTES + NB * B_TILE;  // bytes the TMA writes per stage
     static constexpr uint32_t STAGE_BYTES = (LOAD_BYTES + 1023u) & ~1023u;
-    static constexpr int TAPS = COLS ? 3 : 9;                     // K blocks per input channel block
-    // one persistent CTA per SM: as many stages as fit in ~190 KB, at most 8
-    static constexpr int STAGES = (194560u / STAGE_BYTES > 8) ? 8 : (int)(194560u / STAGE_BYTES);
+    static constexpr int TAPS = MODE == 2 ? 1 : (MODE == 1 ? 3 : 9);  // K blocks per input channel block
+    // one persistent CTA per SM: as many stages as fit in ~208 KB, at most 8
+    static constexpr uint32_t BUDGET = 212992u;
+    static constexpr int STAGES = (BUDGET / STAGE_BYTES > 8) ? 8 : (int)(BUDGET / STAGE_BYTES);
     static constexpr uint32_t SMEM = STAGES * STAGE_BYTES + 1024u;
     static constexpr uint32_t TMEM_COLS = 2u * R * BN;  // two sets of R accumulators
-    static_assert(!COLS || (A_BYTES % 1024u == 0 && B_TILE % 1024u == 0), "COLS tiles must stay 1024-byte aligned");
+    static_assert(MODE == 0 || (A_ROW % 512u == 0 && A_BYTES % 1024u == 0 && B_TILE % 1024u == 0),
+                  "tap-reuse tiles must stay swizzle-aligned");
+    static_assert(STAGES >= 2, "at least two stages");
 };
-
-__device__ __forceinline__ void store_bf16x32(bf16* dst, const float (&v)[32]) {
-    uint4* d = reinterpret_cast<uint4*>(dst);
-#pragma unroll
-    for (int q = 0; q < 4; q++) {
-        __nv_bfloat162 h[4];
-#pragma unroll
-        for (int j = 0; j < 4; j++) h[j] = __floats2bfloat162_rn(v[8 * q + 2 * j], v[8 * q + 2 * j + 1]);
-        d[q] = *reinterpret_cast<uint4*>(h);
-    }
-}
-
-__device__ __forceinline__ void load_bf16x32(const bf16* src, float (&v)[32]) {
-    const uint4* s = reinterpret_cast<const uint4*>(src);
-#pragma unroll
-    for (int q = 0; q < 4; q++) {
-        uint4 u = s[q];
-        const __nv_bfloat162* h = reinterpret_cast<const __nv_bfloat162*>(&u);
-#pragma unroll
-        for (int j = 0; j < 4; j++) {
-            float2 f = __bfloat1622float2(h[j]);
-            v[8 * q + 2 * j] = f.x;
-            v[8 * q + 2 * j + 1] = f.y;
-        }
-    }
-}
 
 __device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
     asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(tc::smem_u32(bar)) : "memory");
@@ -138,8 +122,7 @@ __device__ __forceinline__ void load_bf16x16(const bf16* src, float (&v)[16]) {
     }
 }
 
-constexpr int kEpiWarps = 8;
-constexpr bool kColumnTapReuse = true;  // two warps per TMEM lane quarter, each half of the columns
+constexpr int kEpiWarps = 8;  // two warps per TMEM lane quarter, each half of the columns
 
 // Persistent: one CTA per SM walks the tiles (R rows x 128-pixel segment x BN
 // output channels) t = blockIdx.x, blockIdx.x + gridDim.x, ...
@@ -147,10 +130,10 @@ constexpr bool kColumnTapReuse = true;  // two warps per TMEM lane quarter, each
 // w / 4), warp 8 lane 0: TMA producer over a ring of stages that runs across
 // tiles, warp 9 lane 0: MMA issuer. Two TMEM accumulators: the MMAs of tile
 // i + 1 run while the epilogue drains tile i (acc_full / acc_empty barriers).
-template <int BK, int BN, bool COLS>
+template <int BK, int BN, int MODE>
 __global__ void __launch_bounds__(320, 1) conv3x3_tc(const __grid_constant__ CUtensorMap tmA,
                                                      const __grid_constant__ CUtensorMap tmB, conv_args p) {
-    using C = conv_cfg<BK, BN, COLS>;
+    using C = conv_cfg<BK, BN, MODE>;
     extern __shared__ uint8_t smem_dyn[];
     uint8_t* base = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_dyn) + 1023) & ~(uintptr_t)1023);
     __shared__ uint64_t full[C::STAGES], empty[C::STAGES], acc_full[2], acc_empty[2];
@@ -201,7 +184,13 @@ __global__ void __launch_bounds__(320, 1) conv3x3_tc(const __grid_constant__ CUt
                     const int tap = kb / kpt, cb = kb - tap * kpt;
                     uint8_t* sa = base + (size_t)s * C::STAGE_BYTES;
                     tc::mbar_expect_tx(&full[s], C::LOAD_BYTES);
-                    if (COLS) {
+                    if (MODE == 2) {
+                        // rows y - 1 .. y + R, pixels x0 - 1 .. x0 + 134, all nine taps' weights
+                        tc::tma_load_4d(sa, &tmA, &full[s], p.cin_off + cb * BK, xt * 128 - 1, y - 1, img);
+#pragma unroll
+                        for (int t9 = 0; t9 < 9; t9++)
+                            tc::tma_load_2d(sa + C::A_BYTES + t9 * C::B_TILE, &tmB, &full[s], t9 * p.cin + cb * BK, n0);
+                    } else if (MODE == 1) {
                         // tap = dy row: pixels x0 - 1 .. x0 + 134, the three column taps' weights
                         tc::tma_load_4d(sa, &tmA, &full[s], p.cin_off + cb * BK, xt * 128 - 1, y + tap - 1, img);
 #pragma unroll
@@ -247,13 +236,16 @@ __global__ void __launch_bounds__(320, 1) conv3x3_tc(const __grid_constant__ CUt
 #pragma unroll
                     for (int r = 0; r < C::R; r++)
 #pragma unroll
-                        for (int dx = 0; dx < C::NB; dx++)
+                        for (int t = 0; t < C::NB; t++) {
+                            // MODE 2: tap t = (dy, dx) reads row r + dy; MODE 1: t = dx
+                            const int dy = MODE == 2 ? t / 3 : 0, dx = MODE == 2 ? t % 3 : t;
 #pragma unroll
                             for (int kk = 0; kk < BK / 16; kk++)
                                 tc::mma_bf16(acc + (uint32_t)(r * BN),
-                                             tc::smem_desc_at(sa + r * C::A_ROW + dx * (BK * 2) + kk * 32, BK * 2),
-                                             tc::smem_desc(sb + dx * C::B_TILE + kk * 32, BK * 2), idesc,
-                                             (kb | dx | kk) != 0 ? 1u : 0u);
+                                             tc::smem_desc_at(sa + (r + dy) * C::A_ROW + dx * (BK * 2) + kk * 32, BK * 2),
+                                             tc::smem_desc(sb + t * C::B_TILE + kk * 32, BK * 2), idesc,
+                                             (kb | t | kk) != 0 ? 1u : 0u);
+                        }
                     tc::mma_commit(&empty[s]);
                 }
                 tc::mma_commit(&acc_full[b]);  // also on failure: arrives once the issued MMAs are done
@@ -514,17 +506,17 @@ int sm_count_cached() {
     return n;
 }
 
-template <int BK, int BN, bool COLS>
+template <int BK, int BN, int MODE>
 cudaError_t launch_conv(const CUtensorMap& a, const CUtensorMap& b, const conv_args& p, cudaStream_t s) {
-    using C = conv_cfg<BK, BN, COLS>;
+    using C = conv_cfg<BK, BN, MODE>;
     static std::once_flag once;
     static cudaError_t attr = cudaSuccess;
-    std::call_once(once, [] { attr = raise_smem(conv3x3_tc<BK, BN, COLS>, C::SMEM); });
+    std::call_once(once, [] { attr = raise_smem(conv3x3_tc<BK, BN, MODE>, C::SMEM); });
     if (attr != cudaSuccess) return attr;
     const long long tiles = (long long)p.n_img * ((p.h + C::R - 1) / C::R) * p.tiles_x * (p.cout / BN);
     if (tiles > 0x7FFFFFFFLL) return cudaErrorInvalidValue;
     const int grid = (int)std::min<long long>(tiles, sm_count_cached());
-    conv3x3_tc<BK, BN, COLS><<<grid, 32 * (kEpiWarps + 2), C::SMEM, s>>>(a, b, p);
+    conv3x3_tc<BK, BN, MODE><<<grid, 32 * (kEpiWarps + 2), C::SMEM, s>>>(a, b, p);
     return cudaGetLastError();
 }
 
@@ -559,19 +551,21 @@ extern "C" cudaError_t rfk_unet_conv3x3(const void* in, int n_img, int h, int w,
         return cudaErrorInvalidValue;
     if ((reinterpret_cast<uintptr_t>(in) | reinterpret_cast<uintptr_t>(weights) | reinterpret_cast<uintptr_t>(out)) & 63)
         return cudaErrorMisalignedAddress;
-    const int bk = (cin % 64 == 0 && in_coff % 64 == 0) ? 64 : 32;
     const int bn = pick_bn(cout);
-    // narrow layers (several image rows per tile) reuse one input tile for
-    // the three column taps
-    const bool cols = kColumnTapReuse && bn <= 64;
+    // tap reuse: 32 output channels (4 rows per tile) load each input channel
+    // block once for all nine taps (MODE 2, 32-channel K blocks so that three
+    // 70 KB stages fit); 64 (2 rows) once per tap row (MODE 1); wider tiles
+    // (1 row) once per tap (MODE 0)
+    const int mode = bn == 32 ? 2 : (bn == 64 ? 1 : 0);
+    const int bk = (mode != 2 && cin % 64 == 0 && in_coff % 64 == 0) ? 64 : 32;
     CUtensorMap ma, mb;
     const CUtensorMapSwizzle sw = bk == 64 ? CU_TENSOR_MAP_SWIZZLE_128B : CU_TENSOR_MAP_SWIZZLE_64B;
     {
         cuuint64_t dims[4] = {(cuuint64_t)in_cstride, (cuuint64_t)w, (cuuint64_t)h, (cuuint64_t)n_img};
         cuuint64_t str[3] = {(cuuint64_t)in_cstride * 2, (cuuint64_t)w * in_cstride * 2, (cuuint64_t)h * w * in_cstride * 2};
-        // R image rows per tile and pixel lines per row, as conv_cfg<BK, BN, COLS>
-        const cuuint32_t rows = bn >= 128 ? 1u : (cuuint32_t)(128 / bn);
-        cuuint32_t box[4] = {(cuuint32_t)bk, cols ? 136u : 128u, rows, 1};
+        // image rows and pixel lines of an A box, as conv_cfg<BK, BN, MODE>
+        const cuuint32_t rows = (bn >= 128 ? 1u : (cuuint32_t)(128 / bn)) + (mode == 2 ? 2u : 0u);
+        cuuint32_t box[4] = {(cuuint32_t)bk, mode ? 136u : 128u, rows, 1};
         if (!make_map(&ma, in, 4, dims, str, box, sw)) return cudaErrorInvalidValue;
     }
     {
@@ -601,17 +595,16 @@ extern "C" cudaError_t rfk_unet_conv3x3(const void* in, int n_img, int h, int w,
     p.err = err;
     if (bk == 64) {
         switch (bn) {
-        case 256: return launch_conv<64, 256, false>(ma, mb, p, s);
-        case 128: return launch_conv<64, 128, false>(ma, mb, p, s);
-        case 64: return cols ? launch_conv<64, 64, true>(ma, mb, p, s) : launch_conv<64, 64, false>(ma, mb, p, s);
-        default: return cols ? launch_conv<64, 32, true>(ma, mb, p, s) : launch_conv<64, 32, false>(ma, mb, p, s);
+        case 256: return launch_conv<64, 256, 0>(ma, mb, p, s);
+        case 128: return launch_conv<64, 128, 0>(ma, mb, p, s);
+        default: return launch_conv<64, 64, 1>(ma, mb, p, s);
         }
     }
     switch (bn) {
-    case 256: return launch_conv<32, 256, false>(ma, mb, p, s);
-    case 128: return launch_conv<32, 128, false>(ma, mb, p, s);
-    case 64: return cols ? launch_conv<32, 64, true>(ma, mb, p, s) : launch_conv<32, 64, false>(ma, mb, p, s);
-    default: return cols ? launch_conv<32, 32, true>(ma, mb, p, s) : launch_conv<32, 32, false>(ma, mb, p, s);
+    case 256: return launch_conv<32, 256, 0>(ma, mb, p, s);
+    case 128: return launch_conv<32, 128, 0>(ma, mb, p, s);
+    case 64: return launch_conv<32, 64, 1>(ma, mb, p, s);
+    default: return launch_conv<32, 32, 2>(ma, mb, p, s);
     }
 }
 

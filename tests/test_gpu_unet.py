@@ -62,7 +62,8 @@ def _ref_conv(x_nhwc, w_nkc, bias):
 
 
 @pytest.mark.parametrize("n,h,w,cin,cout", [(2, 5, 200, 64, 128), (1, 4, 64, 32, 32), (2, 3, 130, 96, 64),
-                                            (1, 3, 256, 384, 256), (1, 2, 128, 256, 32), (3, 6, 70, 128, 64)])
+                                            (1, 3, 256, 384, 256), (1, 2, 128, 256, 32), (3, 6, 70, 128, 64),
+                                            (2, 9, 260, 96, 32)])
 def test_conv3x3_matches_fp32_reference(n, h, w, cin, cout):
     L = _L()
     g = torch.Generator(device="cuda").manual_seed(n * 1000 + cin + cout)
