@@ -342,6 +342,7 @@ struct wgrad_args {
     int dx;         // tap column offset of this launch (the X copy is shifted by it)
     int kpc;        // K blocks (64-pixel row segments) per CTA
     int total_kb;   // all row segments
+    int a_rows;     // output channels an A box loads (rows of the 128-row A tile; the rest is not read)
     float* dw;      // [cout][9][cin]
     int* err;
 };
@@ -355,8 +356,14 @@ struct wgrad_cfg {
     static constexpr uint32_t SMEM = STAGES * STAGE_BYTES + 1024u;
 };
 
-// grid: x = K split, y = m tile * (cin / BN) + n tile, z = tap row (dy + 1)
-template <int BN>
+// grid: x = K split, y = m tile * (cin / BN) + n tile, z = tap row (dy + 1).
+// PACK (32 output channels): the three tap rows share one launch, rows
+// 32 d .. 32 d + 31 of the A tile holding dY at image row yy - dy (dy = d - 1)
+// against X at row yy, since sum_y dY[y] X[y + dy] = sum_y' dY[y' - dy] X[y']
+// (rows outside the image are TMA zero fill); the A map is then 4D over
+// (x, y, image, channel). Rows of the A tile that no box writes hold stale
+// data; they only reach accumulator rows the epilogue does not read.
+template <int BN, bool PACK>
 __global__ void __launch_bounds__(128) wgrad3x3_tc(const __grid_constant__ CUtensorMap tmA,
                                                    const __grid_constant__ CUtensorMap tmB, wgrad_args p) {
     using C = wgrad_cfg<BN>;
@@ -408,9 +415,14 @@ __global__ void __launch_bounds__(128) wgrad3x3_tc(const __grid_constant__ CUten
             const int im = seg / (segs_x * p.h);
             const int p0 = (int)(((size_t)im * p.h + yy) * p.w + (size_t)xs * 64);
             uint8_t* sa = base + (size_t)s * C::STAGE_BYTES;
-            tc::mbar_expect_tx(&full[s], C::STAGE_BYTES);
-            tc::tma_load_2d(sa, &tmA, &full[s], p0, m0);
-            tc::tma_load_4d(sa + C::A_BYTES, &tmB, &full[s], xs * 64, yy + dy, c0, im);
+            tc::mbar_expect_tx(&full[s], (PACK ? 3u * 32u : (uint32_t)p.a_rows) * 128u + C::B_BYTES);
+            if (PACK) {
+#pragma unroll
+                for (int d = 0; d < 3; d++) tc::tma_load_4d(sa + d * 4096, &tmA, &full[s], xs * 64, yy - (d - 1), im, 0);
+            } else {
+                tc::tma_load_2d(sa, &tmA, &full[s], p0, m0);
+            }
+            tc::tma_load_4d(sa + C::A_BYTES, &tmB, &full[s], xs * 64, PACK ? yy : yy + dy, c0, im);
             issued++;
         }
         if (!ok) {
@@ -443,14 +455,17 @@ __global__ void __launch_bounds__(128) wgrad3x3_tc(const __grid_constant__ CUten
     bool got = tc::mbar_wait(&done, 0);
     got = __all_sync(0xffffffffu, got);
     tc::fence_after();
-    if (got && nk > 0) {
-        const int m = m0 + warp * 32 + lane;
+    // PACK: warp d < 3 holds tap row d of output channels lane; otherwise
+    // accumulator row m is output channel m of tap row blockIdx.z
+    if (got && nk > 0 && (!PACK || warp < 3)) {
+        const int m = PACK ? lane : m0 + warp * 32 + lane;
+        const int t = PACK ? warp * 3 + (p.dx + 1) : tap;
 #pragma unroll 1
         for (int c = 0; c < BN; c += 32) {
             float v[32];
             tc::tmem_ld32(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)c, v);
             if (m < p.cout) {
-                float* dst = p.dw + ((size_t)m * 9 + tap) * p.cin + c0 + c;
+                float* dst = p.dw + ((size_t)m * 9 + t) * p.cin + c0 + c;
 #pragma unroll
                 for (int j = 0; j < 32; j++) atomicAdd(dst + j, v[j]);
             }
@@ -520,16 +535,16 @@ cudaError_t launch_conv(const CUtensorMap& a, const CUtensorMap& b, const conv_a
     return cudaGetLastError();
 }
 
-template <int BN>
+template <int BN, bool PACK>
 cudaError_t launch_wgrad(const CUtensorMap& a, const CUtensorMap& b, const wgrad_args& p, int splits, cudaStream_t s) {
     using C = wgrad_cfg<BN>;
     static std::once_flag once;
     static cudaError_t attr = cudaSuccess;
-    std::call_once(once, [] { attr = raise_smem(wgrad3x3_tc<BN>, C::SMEM); });
+    std::call_once(once, [] { attr = raise_smem(wgrad3x3_tc<BN, PACK>, C::SMEM); });
     if (attr != cudaSuccess) return attr;
     const int mtiles = (p.cout + 127) / 128;
-    dim3 grid((unsigned)splits, (unsigned)(mtiles * (p.cin / BN)), 3u);
-    wgrad3x3_tc<BN><<<grid, 128, C::SMEM, s>>>(a, b, p);
+    dim3 grid((unsigned)splits, (unsigned)(mtiles * (p.cin / BN)), PACK ? 1u : 3u);
+    wgrad3x3_tc<BN, PACK><<<grid, 128, C::SMEM, s>>>(a, b, p);
     return cudaGetLastError();
 }
 
@@ -616,11 +631,20 @@ extern "C" cudaError_t rfk_unet_wgrad3x3(const void* dyT, const void* const* xT,
         if (reinterpret_cast<uintptr_t>(xT[d]) & 63) return cudaErrorMisalignedAddress;
     const int bn = pick_bn(cin);
     const size_t P = (size_t)n_img * h * w;
+    // 32 output channels: the three tap rows packed into one launch's M
+    const bool pack = cout == 32;
+    const int a_rows = cout < 128 ? cout : 128;
     CUtensorMap ma;
-    {
+    if (pack) {
+        // dyT [cout][image][y][x] as a 4D map, one image row x 32 channels per box
+        cuuint64_t dims[4] = {(cuuint64_t)w, (cuuint64_t)h, (cuuint64_t)n_img, (cuuint64_t)cout};
+        cuuint64_t str[3] = {(cuuint64_t)w * 2, (cuuint64_t)h * w * 2, (cuuint64_t)P * 2};
+        cuuint32_t box[4] = {64, 1, 1, 32};
+        if (!make_map(&ma, dyT, 4, dims, str, box, CU_TENSOR_MAP_SWIZZLE_128B)) return cudaErrorInvalidValue;
+    } else {
         cuuint64_t dims[2] = {(cuuint64_t)P, (cuuint64_t)cout};
         cuuint64_t str[1] = {(cuuint64_t)P * 2};
-        cuuint32_t box[2] = {64, 128};
+        cuuint32_t box[2] = {64, (cuuint32_t)a_rows};
         if (!make_map(&ma, dyT, 2, dims, str, box, CU_TENSOR_MAP_SWIZZLE_128B)) return cudaErrorInvalidValue;
     }
     wgrad_args p{};
@@ -630,9 +654,10 @@ extern "C" cudaError_t rfk_unet_wgrad3x3(const void* dyT, const void* const* xT,
     p.cout = cout;
     p.cin = cin;
     p.total_kb = (int)(P / 64);
+    p.a_rows = a_rows;
     // about 8 CTAs per SM over the three launches' taps and tiles
     const int mtiles = (cout + 127) / 128;
-    const int per_split = 3 * mtiles * (cin / bn);
+    const int per_split = (pack ? 1 : 3) * mtiles * (cin / bn);
     int splits = (152 * 8 / 3 + per_split - 1) / per_split;
     if (splits > p.total_kb) splits = p.total_kb;
     if (splits < 1) splits = 1;
@@ -648,11 +673,20 @@ extern "C" cudaError_t rfk_unet_wgrad3x3(const void* dyT, const void* const* xT,
         if (!make_map(&mb, xT[d], 4, dims, str, box, CU_TENSOR_MAP_SWIZZLE_128B)) return cudaErrorInvalidValue;
         p.dx = d - 1;
         cudaError_t e;
-        switch (bn) {
-        case 256: e = launch_wgrad<256>(ma, mb, p, splits, s); break;
-        case 128: e = launch_wgrad<128>(ma, mb, p, splits, s); break;
-        case 64: e = launch_wgrad<64>(ma, mb, p, splits, s); break;
-        default: e = launch_wgrad<32>(ma, mb, p, splits, s); break;
+        if (pack) {
+            switch (bn) {
+            case 256: e = launch_wgrad<256, true>(ma, mb, p, splits, s); break;
+            case 128: e = launch_wgrad<128, true>(ma, mb, p, splits, s); break;
+            case 64: e = launch_wgrad<64, true>(ma, mb, p, splits, s); break;
+            default: e = launch_wgrad<32, true>(ma, mb, p, splits, s); break;
+            }
+        } else {
+            switch (bn) {
+            case 256: e = launch_wgrad<256, false>(ma, mb, p, splits, s); break;
+            case 128: e = launch_wgrad<128, false>(ma, mb, p, splits, s); break;
+            case 64: e = launch_wgrad<64, false>(ma, mb, p, splits, s); break;
+            default: e = launch_wgrad<32, false>(ma, mb, p, splits, s); break;
+            }
         }
         if (e != cudaSuccess) return e;
     }

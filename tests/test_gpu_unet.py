@@ -114,7 +114,7 @@ def test_conv3x3_input_gradient_with_flipped_weights():
 
 
 @pytest.mark.parametrize("n,h,w,cin,cout", [(2, 3, 128, 32, 32), (1, 4, 64, 64, 128), (2, 2, 192, 128, 256),
-                                            (1, 3, 128, 96, 64)])
+                                            (1, 3, 128, 96, 64), (3, 5, 192, 96, 32)])
 def test_wgrad3x3_matches_fp32_reference(n, h, w, cin, cout):
     L = _L()
     g = torch.Generator(device="cuda").manual_seed(cin * 7 + cout)
