@@ -160,9 +160,29 @@ __device__ __forceinline__ uint64_t smem_desc_at(uint32_t saddr, uint32_t row_by
     return smem_desc(saddr, row_bytes);
 }
 
+// MN-major operand tile (the M or N index contiguous) that TMA wrote as
+// boxes of `row_bytes` (128 or 64, with the matching swizzle) x K rows, one
+// box per group of row_bytes / 2 M or N elements, `group_stride` bytes apart:
+// the stride byte offset is the 8-row K group, the leading byte offset the
+// group stride (checked on the GPU against a reference product for both
+// swizzles and one to four groups).
+__device__ __forceinline__ uint64_t smem_desc_mn(uint32_t saddr, uint32_t row_bytes, uint32_t group_stride) {
+    const uint64_t layout = (row_bytes == 128) ? 2ull : 4ull;
+    uint64_t d = 0;
+    d |= (uint64_t)((saddr >> 4) & 0x3FFFu);
+    d |= (uint64_t)((group_stride >> 4) & 0x3FFFu) << 16;
+    d |= (uint64_t)(((8u * row_bytes) >> 4) & 0x3FFFu) << 32;
+    d |= (uint64_t)1u << 46;
+    d |= layout << 61;
+    return d;
+}
+
 // bf16 x bf16 -> f32, both operands K-major, M x N tile.
 __host__ __device__ constexpr uint32_t idesc_bf16(uint32_t m, uint32_t n) {
     return (1u << 4) | (1u << 7) | (1u << 10) | ((n >> 3) << 17) | ((m >> 4) << 24);
 }
+
+// As idesc_bf16 with the B operand MN-major (bit 16).
+__host__ __device__ constexpr uint32_t idesc_bf16_bmn(uint32_t m, uint32_t n) { return idesc_bf16(m, n) | (1u << 16); }
 
 }  // namespace tc

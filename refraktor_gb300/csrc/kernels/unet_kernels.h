@@ -25,10 +25,10 @@ cudaError_t rfk_unet_conv3x3(const void* in, int n_img, int h, int w, int in_cst
                              cudaStream_t s);
 
 // dW[cout][9][cin] (f32) += sum over pixels of dY[p][n] * X[p + tap][c], on tcgen05. dyT: dY as
-// [cout][n_img * h * w] bf16; xT[d]: X as [n_img][cin][h][w] bf16 shifted by dx = d - 1 columns
-// (rfk_unet_to_chw). w must be a multiple of 64.
-cudaError_t rfk_unet_wgrad3x3(const void* dyT, const void* const* xT, int n_img, int h, int w, int cout, int cin,
-                              float* dw, int* err, cudaStream_t s);
+// [cout][n_img * h * w] bf16 (rfk_unet_to_chw); x: X as NHWC bf16, channels x_coff .. x_coff + cin
+// of x_cstride. w must be a multiple of 64.
+cudaError_t rfk_unet_wgrad3x3(const void* dyT, const void* x, int x_cstride, int x_coff, int n_img, int h, int w, int cout,
+                              int cin, float* dw, int* err, cudaStream_t s);
 
 // Channel-major copy of a channel slice: out[n][c][y][x] = in[n][y][x + dx][coff + c] (0 outside).
 cudaError_t rfk_unet_to_chw(const void* in, int n_img, int h, int w, int cstride, int coff, int c, int dx, void* out,

@@ -19,13 +19,12 @@
 // the weights transposed and the taps flipped ([cin][9][cout]).
 //
 // wgrad3x3_tc (weight gradient): dW[n, t, c] = sum over pixels p of
-// dY[p, n] * X[p + t, c], a GEMM with M = cout (padded to 128 by TMA's zero
-// fill), N = BN input channels, K = pixels, both operands K-major: dY and X
-// are first transposed to channel-major (CHW) copies; a K block is 64 pixels
-// of one image row (W a multiple of 64). A TMA box may not start at an x
-// (innermost) coordinate that is not a multiple of 16 bytes, so the tap's
-// column offset dx in {-1, 0, 1} is applied when X is transposed (one copy per
-// dx, zero outside the image) and the box moves only by the row offset dy.
+// dY[p, n] * X[p + t, c], a GEMM with M = cout (up to 128 per tile), N = BN
+// input channels, K = pixels; a K block is 64 pixels of one image row (W a
+// multiple of 64). A is K-major from a channel-major copy of dY; B is read
+// MN-major straight from the NHWC input: boxes of 32 or 64 channels x 64
+// pixels at the tap's offset, the column offset dx being a pixel coordinate
+// (not the innermost one, so any value is fine; zero fill outside the image).
 // CTAs split K and add their partial sums into dW (f32) atomically.
 #include <cuda.h>
 #include <cuda_bf16.h>
@@ -339,7 +338,8 @@ __global__ void __launch_bounds__(320, 1) conv3x3_tc(const __grid_constant__ CUt
 struct wgrad_args {
     int n_img, h, w;
     int cout, cin;
-    int dx;         // tap column offset of this launch (the X copy is shifted by it)
+    int x_coff;     // first input channel in the NHWC tensor of X
+    int dx;         // tap column offset of this launch
     int kpc;        // K blocks (64-pixel row segments) per CTA
     int total_kb;   // all row segments
     int a_rows;     // output channels an A box loads (rows of the 128-row A tile; the rest is not read)
@@ -351,6 +351,11 @@ template <int BN>
 struct wgrad_cfg {
     static constexpr uint32_t A_BYTES = 128u * 64u * 2u;
     static constexpr uint32_t B_BYTES = (uint32_t)BN * 64u * 2u;
+    // B: groups of G channels (64-byte rows, 64-byte swizzle, for 32-channel
+    // tiles; else 128-byte rows), each a 64-pixel box
+    static constexpr int G = BN == 32 ? 32 : 64;
+    static constexpr uint32_t B_ROW = (uint32_t)G * 2u;
+    static constexpr uint32_t B_GROUP = B_ROW * 64u;
     static constexpr uint32_t STAGE_BYTES = A_BYTES + B_BYTES;
     static constexpr int STAGES = BN == 256 ? 4 : (98304u / STAGE_BYTES > 8 ? 8 : (int)(98304u / STAGE_BYTES));
     static constexpr uint32_t SMEM = STAGES * STAGE_BYTES + 1024u;
@@ -422,7 +427,10 @@ __global__ void __launch_bounds__(128) wgrad3x3_tc(const __grid_constant__ CUten
             } else {
                 tc::tma_load_2d(sa, &tmA, &full[s], p0, m0);
             }
-            tc::tma_load_4d(sa + C::A_BYTES, &tmB, &full[s], xs * 64, PACK ? yy : yy + dy, c0, im);
+#pragma unroll
+            for (int j = 0; j < BN / C::G; j++)
+                tc::tma_load_4d(sa + C::A_BYTES + j * C::B_GROUP, &tmB, &full[s], p.x_coff + c0 + j * C::G,
+                                xs * 64 + p.dx, PACK ? yy : yy + dy, im);
             issued++;
         }
         if (!ok) {
@@ -431,7 +439,7 @@ __global__ void __launch_bounds__(128) wgrad3x3_tc(const __grid_constant__ CUten
                 tc::mbar_wait(&full[kb % C::STAGES], (kb / C::STAGES) & 1);
         }
     } else if (warp == 1 && lane == 0) {
-        constexpr uint32_t idesc = tc::idesc_bf16(128, BN);
+        constexpr uint32_t idesc = tc::idesc_bf16_bmn(128, BN);
         bool ok = true;
         for (int kb = 0; kb < nk; kb++) {
             const int s = kb % C::STAGES, r = kb / C::STAGES;
@@ -443,7 +451,8 @@ __global__ void __launch_bounds__(128) wgrad3x3_tc(const __grid_constant__ CUten
             const uint32_t sa = tc::smem_u32(base + (size_t)s * C::STAGE_BYTES), sb = sa + C::A_BYTES;
 #pragma unroll
             for (int kk = 0; kk < 4; kk++)
-                tc::mma_bf16(tmem, tc::smem_desc(sa + kk * 32, 128), tc::smem_desc(sb + kk * 32, 128), idesc,
+                tc::mma_bf16(tmem, tc::smem_desc(sa + kk * 32, 128), tc::smem_desc_mn(sb + kk * 16 * C::B_ROW, C::B_ROW, C::B_GROUP),
+                             idesc,
                              (kb | kk) != 0 ? 1u : 0u);
             tc::mma_commit(&empty[s]);
         }
@@ -623,18 +632,17 @@ extern "C" cudaError_t rfk_unet_conv3x3(const void* in, int n_img, int h, int w,
     }
 }
 
-extern "C" cudaError_t rfk_unet_wgrad3x3(const void* dyT, const void* const* xT, int n_img, int h, int w, int cout,
-                                         int cin, float* dw, int* err, cudaStream_t s) {
+extern "C" cudaError_t rfk_unet_wgrad3x3(const void* dyT, const void* x, int x_cstride, int x_coff, int n_img, int h, int w,
+                                         int cout, int cin, float* dw, int* err, cudaStream_t s) {
     if (w % 64 || cin % 32 || cout <= 0 || cout % 8 || n_img <= 0 || h <= 0) return cudaErrorInvalidValue;
-    if (reinterpret_cast<uintptr_t>(dyT) & 63) return cudaErrorMisalignedAddress;
-    for (int d = 0; d < 3; d++)
-        if (reinterpret_cast<uintptr_t>(xT[d]) & 63) return cudaErrorMisalignedAddress;
+    if (x_coff % 32 || x_cstride % 32 || x_coff + cin > x_cstride) return cudaErrorInvalidValue;
+    if ((reinterpret_cast<uintptr_t>(dyT) | reinterpret_cast<uintptr_t>(x)) & 63) return cudaErrorMisalignedAddress;
     const int bn = pick_bn(cin);
     const size_t P = (size_t)n_img * h * w;
     // 32 output channels: the three tap rows packed into one launch's M
     const bool pack = cout == 32;
     const int a_rows = cout < 128 ? cout : 128;
-    CUtensorMap ma;
+    CUtensorMap ma, mb;
     if (pack) {
         // dyT [cout][image][y][x] as a 4D map, one image row x 32 channels per box
         cuuint64_t dims[4] = {(cuuint64_t)w, (cuuint64_t)h, (cuuint64_t)n_img, (cuuint64_t)cout};
@@ -647,12 +655,22 @@ extern "C" cudaError_t rfk_unet_wgrad3x3(const void* dyT, const void* const* xT,
         cuuint32_t box[2] = {64, (cuuint32_t)a_rows};
         if (!make_map(&ma, dyT, 2, dims, str, box, CU_TENSOR_MAP_SWIZZLE_128B)) return cudaErrorInvalidValue;
     }
+    {
+        // X NHWC: boxes of 32 (64-byte swizzle) or 64 channels x 64 pixels
+        const cuuint32_t g = bn == 32 ? 32u : 64u;
+        cuuint64_t dims[4] = {(cuuint64_t)x_cstride, (cuuint64_t)w, (cuuint64_t)h, (cuuint64_t)n_img};
+        cuuint64_t str[3] = {(cuuint64_t)x_cstride * 2, (cuuint64_t)w * x_cstride * 2, (cuuint64_t)h * w * x_cstride * 2};
+        cuuint32_t box[4] = {g, 64, 1, 1};
+        if (!make_map(&mb, x, 4, dims, str, box, g == 32 ? CU_TENSOR_MAP_SWIZZLE_64B : CU_TENSOR_MAP_SWIZZLE_128B))
+            return cudaErrorInvalidValue;
+    }
     wgrad_args p{};
     p.n_img = n_img;
     p.h = h;
     p.w = w;
     p.cout = cout;
     p.cin = cin;
+    p.x_coff = x_coff;
     p.total_kb = (int)(P / 64);
     p.a_rows = a_rows;
     // about 8 CTAs per SM over the three launches' taps and tiles
@@ -666,11 +684,6 @@ extern "C" cudaError_t rfk_unet_wgrad3x3(const void* dyT, const void* const* xT,
     p.dw = dw;
     p.err = err;
     for (int d = 0; d < 3; d++) {
-        CUtensorMap mb;
-        cuuint64_t dims[4] = {(cuuint64_t)w, (cuuint64_t)h, (cuuint64_t)cin, (cuuint64_t)n_img};
-        cuuint64_t str[3] = {(cuuint64_t)w * 2, (cuuint64_t)h * w * 2, (cuuint64_t)cin * h * w * 2};
-        cuuint32_t box[4] = {64, 1, (cuuint32_t)bn, 1};
-        if (!make_map(&mb, xT[d], 4, dims, str, box, CU_TENSOR_MAP_SWIZZLE_128B)) return cudaErrorInvalidValue;
         p.dx = d - 1;
         cudaError_t e;
         if (pack) {

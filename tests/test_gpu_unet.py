@@ -22,8 +22,8 @@ def _L():
                                    C.c_void_p, C.c_int, C.c_void_p, C.c_int, C.c_int, C.c_void_p, C.c_int, C.c_int,
                                    C.c_int, C.c_void_p, C.c_void_p]
     L.rfk_unet_wgrad3x3.restype = C.c_int
-    L.rfk_unet_wgrad3x3.argtypes = [C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_void_p,
-                                    C.c_void_p, C.c_void_p]
+    L.rfk_unet_wgrad3x3.argtypes = [C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int,
+                                    C.c_int, C.c_void_p, C.c_void_p, C.c_void_p]
     L.rfk_unet_to_chw.restype = C.c_int
     L.rfk_unet_to_chw.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_void_p,
                                   C.c_void_p]
@@ -120,15 +120,15 @@ def test_wgrad3x3_matches_fp32_reference(n, h, w, cin, cout):
     g = torch.Generator(device="cuda").manual_seed(cin * 7 + cout)
     x = torch.randn(n, h, w, cin, device="cuda", generator=g).to(torch.bfloat16)
     dy = torch.randn(n, h, w, cout, device="cuda", generator=g).to(torch.bfloat16)
-    xT = [torch.empty(n, cin, h, w, dtype=torch.bfloat16, device="cuda") for _ in range(3)]
-    for d in range(3):
-        assert L.rfk_unet_to_chw(x.data_ptr(), n, h, w, cin, 0, cin, d - 1, xT[d].data_ptr(), None) == 0
     dyT = torch.empty(cout, n * h * w, dtype=torch.bfloat16, device="cuda")
     assert L.rfk_unet_to_chw(dy.data_ptr(), 1, 1, n * h * w, cout, 0, cout, 0, dyT.data_ptr(), None) == 0
-    ptrs = (C.c_void_p * 3)(*[t.data_ptr() for t in xT])
     dw = torch.zeros(cout, 9, cin, dtype=torch.float32, device="cuda")
     err = torch.zeros(1, dtype=torch.int32, device="cuda")
-    assert L.rfk_unet_wgrad3x3(dyT.data_ptr(), ptrs, n, h, w, cout, cin, dw.data_ptr(), err.data_ptr(), None) == 0
+    # X read in place: a channel slice of a wider NHWC tensor
+    wide = torch.randn(n, h, w, cin + 64, device="cuda", generator=g).to(torch.bfloat16)
+    wide[..., 32:32 + cin] = x
+    assert L.rfk_unet_wgrad3x3(dyT.data_ptr(), wide.data_ptr(), cin + 64, 32, n, h, w, cout, cin, dw.data_ptr(),
+                               err.data_ptr(), None) == 0
     torch.cuda.synchronize()
     assert int(err.item()) == 0
     ref = torch.nn.grad.conv2d_weight(x.float().permute(0, 3, 1, 2), (cout, cin, 3, 3), dy.float().permute(0, 3, 1, 2),
