@@ -347,18 +347,27 @@ struct wgrad_args {
     int* err;
 };
 
-template <int BN>
+// DXP (input channel tiles of at most 64): the three column taps share one
+// launch as three B blocks of BN channels (X at pixel offsets -1, 0, +1), so
+// the MMA's N is 3 BN.
+template <int BN, bool DXP>
 struct wgrad_cfg {
+    static constexpr int NB = DXP ? 3 * BN : BN;  // MMA N
     static constexpr uint32_t A_BYTES = 128u * 64u * 2u;
-    static constexpr uint32_t B_BYTES = (uint32_t)BN * 64u * 2u;
+    static constexpr uint32_t B_BYTES = (uint32_t)NB * 64u * 2u;
     // B: groups of G channels (64-byte rows, 64-byte swizzle, for 32-channel
     // tiles; else 128-byte rows), each a 64-pixel box
     static constexpr int G = BN == 32 ? 32 : 64;
     static constexpr uint32_t B_ROW = (uint32_t)G * 2u;
     static constexpr uint32_t B_GROUP = B_ROW * 64u;
     static constexpr uint32_t STAGE_BYTES = A_BYTES + B_BYTES;
-    static constexpr int STAGES = BN == 256 ? 4 : (98304u / STAGE_BYTES > 8 ? 8 : (int)(98304u / STAGE_BYTES));
+    // two CTAs per SM of ~96 KB; packed column taps (bigger stages): one CTA
+    // with a deeper ring
+    static constexpr uint32_t BUDGET = DXP ? 196608u : 98304u;
+    static constexpr int STAGES = BN == 256 ? 4 : (BUDGET / STAGE_BYTES > 8 ? 8 : (int)(BUDGET / STAGE_BYTES));
     static constexpr uint32_t SMEM = STAGES * STAGE_BYTES + 1024u;
+    static constexpr uint32_t TMEM_COLS = NB <= 32 ? 32u : NB <= 64 ? 64u : NB <= 128 ? 128u : 256u;
+    static_assert(!DXP || BN <= 64, "column taps packed only for tiles of at most 64 channels");
 };
 
 // grid: x = K split, y = m tile * (cin / BN) + n tile, z = tap row (dy + 1).
@@ -368,10 +377,10 @@ struct wgrad_cfg {
 // (rows outside the image are TMA zero fill); the A map is then 4D over
 // (x, y, image, channel). Rows of the A tile that no box writes hold stale
 // data; they only reach accumulator rows the epilogue does not read.
-template <int BN, bool PACK>
+template <int BN, bool PACK, bool DXP>
 __global__ void __launch_bounds__(128) wgrad3x3_tc(const __grid_constant__ CUtensorMap tmA,
                                                    const __grid_constant__ CUtensorMap tmB, wgrad_args p) {
-    using C = wgrad_cfg<BN>;
+    using C = wgrad_cfg<BN, DXP>;
     extern __shared__ uint8_t smem_dyn[];
     uint8_t* base = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_dyn) + 1023) & ~(uintptr_t)1023);
     __shared__ uint64_t full[C::STAGES], empty[C::STAGES], done;
@@ -383,14 +392,13 @@ __global__ void __launch_bounds__(128) wgrad3x3_tc(const __grid_constant__ CUten
     const int m0 = (blockIdx.y / ntiles) * 128;
     const int c0 = (blockIdx.y % ntiles) * BN;
     const int dy = (int)blockIdx.z - 1;
-    const int tap = (dy + 1) * 3 + (p.dx + 1);
     const int segs_x = p.w / 64;
     const int kb0 = blockIdx.x * p.kpc;
     int nk = p.total_kb - kb0;
     if (nk > p.kpc) nk = p.kpc;
     if (nk < 0) nk = 0;
 
-    if (warp == 0) tc::tmem_alloc(&tmem_base, BN);
+    if (warp == 0) tc::tmem_alloc(&tmem_base, C::TMEM_COLS);
     if (threadIdx.x == 32) {
         for (int s = 0; s < C::STAGES; s++) {
             tc::mbar_init(&full[s], 1);
@@ -428,9 +436,11 @@ __global__ void __launch_bounds__(128) wgrad3x3_tc(const __grid_constant__ CUten
                 tc::tma_load_2d(sa, &tmA, &full[s], p0, m0);
             }
 #pragma unroll
-            for (int j = 0; j < BN / C::G; j++)
-                tc::tma_load_4d(sa + C::A_BYTES + j * C::B_GROUP, &tmB, &full[s], p.x_coff + c0 + j * C::G,
-                                xs * 64 + p.dx, PACK ? yy : yy + dy, im);
+            for (int xi = 0; xi < (DXP ? 3 : 1); xi++)
+#pragma unroll
+                for (int j = 0; j < BN / C::G; j++)
+                    tc::tma_load_4d(sa + C::A_BYTES + (xi * (BN / C::G) + j) * C::B_GROUP, &tmB, &full[s],
+                                    p.x_coff + c0 + j * C::G, xs * 64 + (DXP ? xi - 1 : p.dx), PACK ? yy : yy + dy, im);
             issued++;
         }
         if (!ok) {
@@ -439,7 +449,7 @@ __global__ void __launch_bounds__(128) wgrad3x3_tc(const __grid_constant__ CUten
                 tc::mbar_wait(&full[kb % C::STAGES], (kb / C::STAGES) & 1);
         }
     } else if (warp == 1 && lane == 0) {
-        constexpr uint32_t idesc = tc::idesc_bf16_bmn(128, BN);
+        constexpr uint32_t idesc = tc::idesc_bf16_bmn(128, C::NB);
         bool ok = true;
         for (int kb = 0; kb < nk; kb++) {
             const int s = kb % C::STAGES, r = kb / C::STAGES;
@@ -465,16 +475,18 @@ __global__ void __launch_bounds__(128) wgrad3x3_tc(const __grid_constant__ CUten
     got = __all_sync(0xffffffffu, got);
     tc::fence_after();
     // PACK: warp d < 3 holds tap row d of output channels lane; otherwise
-    // accumulator row m is output channel m of tap row blockIdx.z
+    // accumulator row m is output channel m of tap row blockIdx.z. DXP:
+    // columns [xi BN, (xi + 1) BN) belong to column tap xi
     if (got && nk > 0 && (!PACK || warp < 3)) {
         const int m = PACK ? lane : m0 + warp * 32 + lane;
-        const int t = PACK ? warp * 3 + (p.dx + 1) : tap;
+        const int trow = PACK ? warp : dy + 1;
 #pragma unroll 1
-        for (int c = 0; c < BN; c += 32) {
+        for (int c = 0; c < C::NB; c += 32) {
             float v[32];
             tc::tmem_ld32(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)c, v);
+            const int xi = DXP ? c / BN : p.dx + 1, cc = DXP ? c % BN : c;
             if (m < p.cout) {
-                float* dst = p.dw + ((size_t)m * 9 + t) * p.cin + c0 + c;
+                float* dst = p.dw + ((size_t)m * 9 + trow * 3 + xi) * p.cin + c0 + cc;
 #pragma unroll
                 for (int j = 0; j < 32; j++) atomicAdd(dst + j, v[j]);
             }
@@ -483,7 +495,7 @@ __global__ void __launch_bounds__(128) wgrad3x3_tc(const __grid_constant__ CUten
     tc::fence_before();
     __syncthreads();
     if (threadIdx.x == 0 && (!got || s_fail)) atomicExch(p.err, 1);
-    if (warp == 0) tc::tmem_dealloc(tmem, BN);
+    if (warp == 0) tc::tmem_dealloc(tmem, C::TMEM_COLS);
 }
 
 // ------------------------------------------------------------- tensor maps --
@@ -544,16 +556,16 @@ cudaError_t launch_conv(const CUtensorMap& a, const CUtensorMap& b, const conv_a
     return cudaGetLastError();
 }
 
-template <int BN, bool PACK>
+template <int BN, bool PACK, bool DXP>
 cudaError_t launch_wgrad(const CUtensorMap& a, const CUtensorMap& b, const wgrad_args& p, int splits, cudaStream_t s) {
-    using C = wgrad_cfg<BN>;
+    using C = wgrad_cfg<BN, DXP>;
     static std::once_flag once;
     static cudaError_t attr = cudaSuccess;
-    std::call_once(once, [] { attr = raise_smem(wgrad3x3_tc<BN, PACK>, C::SMEM); });
+    std::call_once(once, [] { attr = raise_smem(wgrad3x3_tc<BN, PACK, DXP>, C::SMEM); });
     if (attr != cudaSuccess) return attr;
     const int mtiles = (p.cout + 127) / 128;
     dim3 grid((unsigned)splits, (unsigned)(mtiles * (p.cin / BN)), PACK ? 1u : 3u);
-    wgrad3x3_tc<BN, PACK><<<grid, 128, C::SMEM, s>>>(a, b, p);
+    wgrad3x3_tc<BN, PACK, DXP><<<grid, 128, C::SMEM, s>>>(a, b, p);
     return cudaGetLastError();
 }
 
@@ -674,8 +686,10 @@ extern "C" cudaError_t rfk_unet_wgrad3x3(const void* dyT, const void* x, int x_c
     p.total_kb = (int)(P / 64);
     p.a_rows = a_rows;
     // about 8 CTAs per SM over the three launches' taps and tiles
+    // input channel tiles of at most 64: the column taps packed into N
+    const bool dxp = bn <= 64;
     const int mtiles = (cout + 127) / 128;
-    const int per_split = (pack ? 1 : 3) * mtiles * (cin / bn);
+    const int per_split = (pack ? 1 : 3) * (dxp ? 1 : 3) * mtiles * (cin / bn);
     int splits = (152 * 8 / 3 + per_split - 1) / per_split;
     if (splits > p.total_kb) splits = p.total_kb;
     if (splits < 1) splits = 1;
@@ -683,23 +697,16 @@ extern "C" cudaError_t rfk_unet_wgrad3x3(const void* dyT, const void* x, int x_c
     splits = (p.total_kb + p.kpc - 1) / p.kpc;
     p.dw = dw;
     p.err = err;
-    for (int d = 0; d < 3; d++) {
+    for (int d = 0; d < (dxp ? 1 : 3); d++) {
         p.dx = d - 1;
         cudaError_t e;
-        if (pack) {
-            switch (bn) {
-            case 256: e = launch_wgrad<256, true>(ma, mb, p, splits, s); break;
-            case 128: e = launch_wgrad<128, true>(ma, mb, p, splits, s); break;
-            case 64: e = launch_wgrad<64, true>(ma, mb, p, splits, s); break;
-            default: e = launch_wgrad<32, true>(ma, mb, p, splits, s); break;
-            }
+        if (dxp) {
+            if (bn == 64) e = pack ? launch_wgrad<64, true, true>(ma, mb, p, splits, s) : launch_wgrad<64, false, true>(ma, mb, p, splits, s);
+            else e = pack ? launch_wgrad<32, true, true>(ma, mb, p, splits, s) : launch_wgrad<32, false, true>(ma, mb, p, splits, s);
+        } else if (pack) {
+            e = bn == 256 ? launch_wgrad<256, true, false>(ma, mb, p, splits, s) : launch_wgrad<128, true, false>(ma, mb, p, splits, s);
         } else {
-            switch (bn) {
-            case 256: e = launch_wgrad<256, false>(ma, mb, p, splits, s); break;
-            case 128: e = launch_wgrad<128, false>(ma, mb, p, splits, s); break;
-            case 64: e = launch_wgrad<64, false>(ma, mb, p, splits, s); break;
-            default: e = launch_wgrad<32, false>(ma, mb, p, splits, s); break;
-            }
+            e = bn == 256 ? launch_wgrad<256, false, false>(ma, mb, p, splits, s) : launch_wgrad<128, false, false>(ma, mb, p, splits, s);
         }
         if (e != cudaSuccess) return e;
     }
