@@ -83,7 +83,6 @@ struct workspace {
     bf16 *gl2a, *gl2b, *g_cat2, *g_p1;
     bf16 *gl3a, *gl3b, *g_cat3, *g_p2;
     bf16 *gl4a, *gl4b, *g_p3;
-    bf16* dyT;    // largest dY^T (the weight gradient reads X in place)
     float4* target_scratch = nullptr;
     ~workspace() {
         for (void* p : owned) cudaFree(p);
@@ -159,11 +158,6 @@ struct rfk_denoiser {
             s->gl4a = s->take<bf16>(P4 * 256);
             s->gl4b = s->take<bf16>(P4 * 256);
             s->g_p3 = s->take<bf16>(P4 * 128);
-            // largest (channels x pixels) among the layers' dY
-            size_t dy_max = 0;
-            const size_t px[NLAYERS] = {P1, P1, P2, P2, P3, P3, P4, P4, P3, P3, P2, P2, P1, P1, P1};
-            for (int l = 0; l < NLAYERS; l++) dy_max = std::max(dy_max, px[l] * kLayers[l].cout);
-            s->dyT = s->take<bf16>(dy_max);
         }
         workspace& r = *s;
         ws[key] = std::move(s);
@@ -214,8 +208,7 @@ struct rfk_denoiser {
         const layer& y = L[l];
         const size_t P = (size_t)n * h * w;
         cuda_check(rfk_unet_bias_grad(dy, P, y.d.cout, y.bg, st), "bias grad");
-        cuda_check(rfk_unet_to_chw(dy, 1, 1, (int)P, y.d.cout, 0, y.d.cout, 0, s.dyT, st), "transpose");
-        cuda_check(rfk_unet_wgrad3x3(s.dyT, x, x_cstride, x_coff, n, h, w, y.d.cout, y.d.cin, y.g, d_err, st), "wgrad");
+        cuda_check(rfk_unet_wgrad3x3(dy, x, x_cstride, x_coff, n, h, w, y.d.cout, y.d.cin, y.g, d_err, st), "wgrad");
         if (dx)
             cuda_check(rfk_unet_conv3x3(dy, n, h, w, y.d.cout, 0, y.d.cout, y.wb, y.d.cin, nullptr, 0, dx, dx_cstride, dx_coff,
                                         mask, y.d.cin, 0, 0, d_err, st),

@@ -24,10 +24,10 @@ cudaError_t rfk_unet_conv3x3(const void* in, int n_img, int h, int w, int in_cst
                              int out_coff, const void* mask, int mask_cstride, int mask_coff, int accumulate, int* err,
                              cudaStream_t s);
 
-// dW[cout][9][cin] (f32) += sum over pixels of dY[p][n] * X[p + tap][c], on tcgen05. dyT: dY as
-// [cout][n_img * h * w] bf16 (rfk_unet_to_chw); x: X as NHWC bf16, channels x_coff .. x_coff + cin
-// of x_cstride. w must be a multiple of 64.
-cudaError_t rfk_unet_wgrad3x3(const void* dyT, const void* x, int x_cstride, int x_coff, int n_img, int h, int w, int cout,
+// dW[cout][9][cin] (f32) += sum over pixels of dY[p][n] * X[p + tap][c], on tcgen05. dy: dY as
+// dense NHWC bf16 (cout channels); x: X as NHWC bf16, channels x_coff .. x_coff + cin of
+// x_cstride. w must be a multiple of 64, cin and cout of 32.
+cudaError_t rfk_unet_wgrad3x3(const void* dy, const void* x, int x_cstride, int x_coff, int n_img, int h, int w, int cout,
                               int cin, float* dw, int* err, cudaStream_t s);
 
 // Channel-major copy of a channel slice: out[n][c][y][x] = in[n][y][x + dx][coff + c] (0 outside).

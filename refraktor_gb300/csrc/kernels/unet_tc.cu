@@ -381,6 +381,9 @@ template <int BN, bool PACK, bool DXP>
 __global__ void __launch_bounds__(128) wgrad3x3_tc(const __grid_constant__ CUtensorMap tmA,
                                                    const __grid_constant__ CUtensorMap tmB, wgrad_args p) {
     using C = wgrad_cfg<BN, DXP>;
+    // A (dY, MN-major from NHWC): groups of 32 output channels (64-byte rows)
+    // when packed, else of 64 (128-byte rows); the 128-row tile is 16 KB
+    constexpr uint32_t A_ROW = PACK ? 64u : 128u, A_GROUP = A_ROW * 64u;
     extern __shared__ uint8_t smem_dyn[];
     uint8_t* base = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_dyn) + 1023) & ~(uintptr_t)1023);
     __shared__ uint64_t full[C::STAGES], empty[C::STAGES], done;
@@ -426,14 +429,14 @@ __global__ void __launch_bounds__(128) wgrad3x3_tc(const __grid_constant__ CUten
             const int xs = seg % segs_x;
             const int yy = (seg / segs_x) % p.h;
             const int im = seg / (segs_x * p.h);
-            const int p0 = (int)(((size_t)im * p.h + yy) * p.w + (size_t)xs * 64);
             uint8_t* sa = base + (size_t)s * C::STAGE_BYTES;
-            tc::mbar_expect_tx(&full[s], (PACK ? 3u * 32u : (uint32_t)p.a_rows) * 128u + C::B_BYTES);
+            // whole boxes count, zero fill included
+            tc::mbar_expect_tx(&full[s], (PACK ? 3u : (uint32_t)(p.a_rows + 63) / 64u) * A_GROUP + C::B_BYTES);
             if (PACK) {
 #pragma unroll
-                for (int d = 0; d < 3; d++) tc::tma_load_4d(sa + d * 4096, &tmA, &full[s], xs * 64, yy - (d - 1), im, 0);
+                for (int d = 0; d < 3; d++) tc::tma_load_4d(sa + d * A_GROUP, &tmA, &full[s], 0, xs * 64, yy - (d - 1), im);
             } else {
-                tc::tma_load_2d(sa, &tmA, &full[s], p0, m0);
+                for (int j = 0; j * 64 < p.a_rows; j++) tc::tma_load_4d(sa + j * A_GROUP, &tmA, &full[s], m0 + j * 64, xs * 64, yy, im);
             }
 #pragma unroll
             for (int xi = 0; xi < (DXP ? 3 : 1); xi++)
@@ -449,7 +452,7 @@ __global__ void __launch_bounds__(128) wgrad3x3_tc(const __grid_constant__ CUten
                 tc::mbar_wait(&full[kb % C::STAGES], (kb / C::STAGES) & 1);
         }
     } else if (warp == 1 && lane == 0) {
-        constexpr uint32_t idesc = tc::idesc_bf16_bmn(128, C::NB);
+        constexpr uint32_t idesc = tc::idesc_bf16_bmn(128, C::NB) | (1u << 15);  // A MN-major too
         bool ok = true;
         for (int kb = 0; kb < nk; kb++) {
             const int s = kb % C::STAGES, r = kb / C::STAGES;
@@ -461,7 +464,8 @@ __global__ void __launch_bounds__(128) wgrad3x3_tc(const __grid_constant__ CUten
             const uint32_t sa = tc::smem_u32(base + (size_t)s * C::STAGE_BYTES), sb = sa + C::A_BYTES;
 #pragma unroll
             for (int kk = 0; kk < 4; kk++)
-                tc::mma_bf16(tmem, tc::smem_desc(sa + kk * 32, 128), tc::smem_desc_mn(sb + kk * 16 * C::B_ROW, C::B_ROW, C::B_GROUP),
+                tc::mma_bf16(tmem, tc::smem_desc_mn(sa + kk * 16 * A_ROW, A_ROW, A_GROUP),
+                             tc::smem_desc_mn(sb + kk * 16 * C::B_ROW, C::B_ROW, C::B_GROUP),
                              idesc,
                              (kb | kk) != 0 ? 1u : 0u);
             tc::mma_commit(&empty[s]);
@@ -644,28 +648,26 @@ extern "C" cudaError_t rfk_unet_conv3x3(const void* in, int n_img, int h, int w,
     }
 }
 
-extern "C" cudaError_t rfk_unet_wgrad3x3(const void* dyT, const void* x, int x_cstride, int x_coff, int n_img, int h, int w,
+extern "C" cudaError_t rfk_unet_wgrad3x3(const void* dy, const void* x, int x_cstride, int x_coff, int n_img, int h, int w,
                                          int cout, int cin, float* dw, int* err, cudaStream_t s) {
-    if (w % 64 || cin % 32 || cout <= 0 || cout % 8 || n_img <= 0 || h <= 0) return cudaErrorInvalidValue;
+    if (w % 64 || cin % 32 || cout <= 0 || cout % 32 || n_img <= 0 || h <= 0) return cudaErrorInvalidValue;
     if (x_coff % 32 || x_cstride % 32 || x_coff + cin > x_cstride) return cudaErrorInvalidValue;
-    if ((reinterpret_cast<uintptr_t>(dyT) | reinterpret_cast<uintptr_t>(x)) & 63) return cudaErrorMisalignedAddress;
+    if ((reinterpret_cast<uintptr_t>(dy) | reinterpret_cast<uintptr_t>(x)) & 63) return cudaErrorMisalignedAddress;
     const int bn = pick_bn(cin);
     const size_t P = (size_t)n_img * h * w;
     // 32 output channels: the three tap rows packed into one launch's M
     const bool pack = cout == 32;
     const int a_rows = cout < 128 ? cout : 128;
     CUtensorMap ma, mb;
-    if (pack) {
-        // dyT [cout][image][y][x] as a 4D map, one image row x 32 channels per box
-        cuuint64_t dims[4] = {(cuuint64_t)w, (cuuint64_t)h, (cuuint64_t)n_img, (cuuint64_t)cout};
-        cuuint64_t str[3] = {(cuuint64_t)w * 2, (cuuint64_t)h * w * 2, (cuuint64_t)P * 2};
-        cuuint32_t box[4] = {64, 1, 1, 32};
-        if (!make_map(&ma, dyT, 4, dims, str, box, CU_TENSOR_MAP_SWIZZLE_128B)) return cudaErrorInvalidValue;
-    } else {
-        cuuint64_t dims[2] = {(cuuint64_t)P, (cuuint64_t)cout};
-        cuuint64_t str[1] = {(cuuint64_t)P * 2};
-        cuuint32_t box[2] = {64, (cuuint32_t)a_rows};
-        if (!make_map(&ma, dyT, 2, dims, str, box, CU_TENSOR_MAP_SWIZZLE_128B)) return cudaErrorInvalidValue;
+    {
+        // dY NHWC (cout channels): boxes of 32 (packed, 64-byte swizzle) or 64
+        // output channels x 64 pixels, MN-major
+        const cuuint32_t g = pack ? 32u : 64u;
+        cuuint64_t dims[4] = {(cuuint64_t)cout, (cuuint64_t)w, (cuuint64_t)h, (cuuint64_t)n_img};
+        cuuint64_t str[3] = {(cuuint64_t)cout * 2, (cuuint64_t)w * cout * 2, (cuuint64_t)h * w * cout * 2};
+        cuuint32_t box[4] = {g, 64, 1, 1};
+        if (!make_map(&ma, dy, 4, dims, str, box, pack ? CU_TENSOR_MAP_SWIZZLE_64B : CU_TENSOR_MAP_SWIZZLE_128B))
+            return cudaErrorInvalidValue;
     }
     {
         // X NHWC: boxes of 32 (64-byte swizzle) or 64 channels x 64 pixels

@@ -120,14 +120,12 @@ def test_wgrad3x3_matches_fp32_reference(n, h, w, cin, cout):
     g = torch.Generator(device="cuda").manual_seed(cin * 7 + cout)
     x = torch.randn(n, h, w, cin, device="cuda", generator=g).to(torch.bfloat16)
     dy = torch.randn(n, h, w, cout, device="cuda", generator=g).to(torch.bfloat16)
-    dyT = torch.empty(cout, n * h * w, dtype=torch.bfloat16, device="cuda")
-    assert L.rfk_unet_to_chw(dy.data_ptr(), 1, 1, n * h * w, cout, 0, cout, 0, dyT.data_ptr(), None) == 0
     dw = torch.zeros(cout, 9, cin, dtype=torch.float32, device="cuda")
     err = torch.zeros(1, dtype=torch.int32, device="cuda")
     # X read in place: a channel slice of a wider NHWC tensor
     wide = torch.randn(n, h, w, cin + 64, device="cuda", generator=g).to(torch.bfloat16)
     wide[..., 32:32 + cin] = x
-    assert L.rfk_unet_wgrad3x3(dyT.data_ptr(), wide.data_ptr(), cin + 64, 32, n, h, w, cout, cin, dw.data_ptr(),
+    assert L.rfk_unet_wgrad3x3(dy.data_ptr(), wide.data_ptr(), cin + 64, 32, n, h, w, cout, cin, dw.data_ptr(),
                                err.data_ptr(), None) == 0
     torch.cuda.synchronize()
     assert int(err.item()) == 0
