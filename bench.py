@@ -52,6 +52,38 @@ def _dist():
     return ws, rank
 
 
+def _init_dist(ws: int, backend: str = "nccl") -> None:
+    """One process per GPU under torchrun: the process group for the barrier
+    and the rank totals (no data-path collective: ranks are replicas)."""
+    if ws > 1:
+        import torch.distributed as dist
+
+        if not dist.is_initialized():
+            dist.init_process_group(backend)
+
+
+def _barrier(ws: int) -> None:
+    if ws > 1:
+        import torch.distributed as dist
+
+        dist.barrier()
+
+
+def merge_ranks(seconds: float, counts: list, device: str = "cuda") -> tuple:
+    """Whole-job totals of a replicas-only run: the slowest rank's time (all
+    ranks start together after a barrier, so the job ends with it) and the
+    sum of every rank's counts. One process per GPU; a no-op for one rank."""
+    import torch
+
+    if not torch.distributed.is_available() or not torch.distributed.is_initialized():
+        return seconds, list(counts)
+    t = torch.tensor([seconds], device=device, dtype=torch.float64)
+    torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+    c = torch.tensor([float(x) for x in counts], device=device, dtype=torch.float64)
+    torch.distributed.all_reduce(c)
+    return float(t.item()), [int(x) for x in c.tolist()]
+
+
 class ClockSampler:
     """nvidia-smi samples of SM clock and throttle reasons during the timed region."""
 
@@ -117,10 +149,7 @@ def run_gpu(args) -> dict:
 
     ws, rank = _dist()
     torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
-    if ws > 1:
-        import torch.distributed as dist
-
-        dist.init_process_group("nccl")
+    _init_dist(ws)
     build.build()
     db = lr.flamedb()
     genome = load_workload()
@@ -156,13 +185,7 @@ def run_gpu(args) -> dict:
             draws += r.draw_count
             elapsed_kernel += r.elapsed_ms / 1e3
     t_total = sum(times)
-    if ws > 1:
-        t = torch.tensor([t_total], device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        t_total = float(t.item())
-        pt = torch.tensor([passes, draws], device="cuda", dtype=torch.float64)
-        torch.distributed.all_reduce(pt)
-        passes, draws = int(pt[0].item()), int(pt[1].item())
+    t_total, (passes, draws) = merge_ranks(t_total, [passes, draws])
     value = passes / t_total
     bin_launch_s = t_total / args.steps
 
@@ -195,13 +218,7 @@ def run_gpu(args) -> dict:
             e2e_times.append(dt)
             e2e_passes += r.total_passes + k.info["grid"] * k.info["block"] * WARMUP_PASSES
     e2e_t = sum(e2e_times)
-    if ws > 1:
-        t = torch.tensor([e2e_t], device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        e2e_t = float(t.item())
-        pt = torch.tensor([e2e_passes], device="cuda", dtype=torch.float64)
-        torch.distributed.all_reduce(pt)
-        e2e_passes = int(pt.item())
+    e2e_t, (e2e_passes,) = merge_ranks(e2e_t, [e2e_passes])
 
     line = {
         "metric": METRIC,
@@ -315,7 +332,9 @@ def run_batch(args) -> dict:
     from refraktor_gb300 import build
     from refraktor_gb300 import librefrakt as lr
 
+    ws, rank = _dist()
     torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+    _init_dist(ws)
     build.build()
     db = lr.flamedb()
     kf, samples, units, text, (tf, tsamples, tdims) = batch_workload(lr, db, args.workload)
@@ -353,6 +372,7 @@ def run_batch(args) -> dict:
         for _ in range(args.steps):
             _flush_l2(flush)
             torch.cuda.synchronize()
+            _barrier(ws)
             e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
             e0.record(stream)
             b.run(use_graph=True, stream=stream)
@@ -363,7 +383,7 @@ def run_batch(args) -> dict:
             draws += tot.draw_count
             kern_ms += tot.elapsed_ms
             reached = reached and bool(tot.status & 1)
-    t_total = sum(times)
+    t_total, (passes, draws) = merge_ranks(sum(times), [passes, draws])
     info = b.info()
 
     # e2e: host samples in, every tonemapped image out (pinned)
@@ -373,6 +393,7 @@ def run_batch(args) -> dict:
     for i in range(args.warmup + args.steps):
         _flush_l2(flush)
         torch.cuda.synchronize()
+        _barrier(ws)
         t0 = time.perf_counter()
         b.set_samples(samples)
         b.run(use_graph=True, stream=stream)
@@ -383,11 +404,13 @@ def run_batch(args) -> dict:
         if i >= args.warmup:
             e2e_times.append(time.perf_counter() - t0)
             e2e_passes += tot.total_passes
-    e2e_t = sum(e2e_times)
+    e2e_t, (e2e_passes,) = merge_ranks(sum(e2e_times), [e2e_passes])
     peak_ops = lr.probe_red_v4(8 << 20, 512)
     achieved_ops = draws / max(kern_ms / 1e3, 1e-9)
+    if rank != 0:
+        return {}
     return {
-        "metric": METRIC, "value": passes / t_total, "unit": "iterations/s", "n_gpus": 1, "steps": args.steps,
+        "metric": METRIC, "value": passes / t_total, "unit": "iterations/s", "n_gpus": ws, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": 1e3 * t_total / args.steps, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded genomes refraktor_gb300/workloads/)",
         "config": {"workload": text, "units": len(units), "pixels": int(sum(u.width * u.height for u in units)),
@@ -422,6 +445,10 @@ def run_denoise(args) -> dict:
     from refraktor_gb300 import librefrakt as lr
     from refraktor_gb300.workloads import train_denoiser as td
 
+    ws, rank = _dist()
+    if rank != 0:
+        # a fixed evaluation set, not sharded: the other ranks have no work
+        return {}
     torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
     build.build()
     db = lr.flamedb()
