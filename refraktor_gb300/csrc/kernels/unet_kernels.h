@@ -30,12 +30,6 @@ cudaError_t rfk_unet_conv3x3(const void* in, int n_img, int h, int w, int in_cst
 cudaError_t rfk_unet_wgrad3x3(const void* dy, const void* x, int x_cstride, int x_coff, int n_img, int h, int w, int cout,
                               int cin, float* dw, int* err, cudaStream_t s);
 
-// Channel-major copy of a channel slice: out[n][c][y][x] = in[n][y][x + dx][coff + c] (0 outside).
-cudaError_t rfk_unet_to_chw(const void* in, int n_img, int h, int w, int cstride, int coff, int c, int dx, void* out,
-                            cudaStream_t s);
-// The same for nshift (1..3) shifts dx0, dx0 + 1, ... into out0, out1, out2 in one pass.
-cudaError_t rfk_unet_to_chw3(const void* in, int n_img, int h, int w, int cstride, int coff, int c, int dx0, int nshift,
-                             void* out0, void* out1, void* out2, cudaStream_t s);
 
 // Network input (32 bf16 channels per pixel) of a float4 histogram rendered at `spp` and its
 // tonemapped image `base` (float4).

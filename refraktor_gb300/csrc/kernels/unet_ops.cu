@@ -9,68 +9,6 @@ namespace {
 
 using bf16 = __nv_bfloat16;
 
-// Channel-major copies of a channel slice, one per column shift dx in
-// [dx0, dx0 + nshift): a block stages 64 + 2 pixels of one row x 32 channels
-// in shared memory (16-byte loads along channels) and writes each shifted copy
-// with 16-byte stores along x.
-__global__ void to_chw_kernel(const bf16* __restrict__ in, int h, int w, int cstride, int coff, int c, int dx0, int nshift,
-                              bf16* __restrict__ out0, bf16* __restrict__ out1, bf16* __restrict__ out2) {
-    __shared__ __align__(16) bf16 t[66][40];  // [x + 1][channel], rows padded against bank conflicts
-    const int xb = blockIdx.x * 64, ny = blockIdx.y, cb = blockIdx.z * 32;
-    const int n = ny / h, y = ny - n * h;
-    // load: 66 pixels x 4 chunks of 8 channels
-    for (int i = threadIdx.x; i < 66 * 4; i += blockDim.x) {
-        const int px = i >> 2, q = i & 3, x = xb + px - 1, ch = cb + q * 8;
-        uint4 v = make_uint4(0, 0, 0, 0);
-        if (x >= 0 && x < w && ch < c) v = *reinterpret_cast<const uint4*>(in + ((size_t)ny * w + x) * cstride + coff + ch);
-        *reinterpret_cast<uint4*>(&t[px][q * 8]) = v;
-    }
-    __syncthreads();
-    // store: per shift, 32 channels x 8 chunks of 8 pixels
-    bf16* outs[3] = {out0, out1, out2};
-    for (int sft = 0; sft < nshift; sft++) {
-        const int dx = dx0 + sft;
-        for (int i = threadIdx.x; i < 32 * 8; i += blockDim.x) {
-            const int ch = cb + (i >> 3), x8 = (i & 7) * 8, x = xb + x8;
-            if (ch >= c || x >= w) continue;
-            __align__(16) bf16 v[8];
-#pragma unroll
-            for (int j = 0; j < 8; j++) {
-                const int sx = x + j + dx;
-                v[j] = (sx >= 0 && sx < w) ? t[x8 + j + dx + 1][ch - cb] : __float2bfloat16(0.0f);
-            }
-            bf16* dst = outs[sft] + (((size_t)n * c + ch) * h + y) * w + x;
-            if (x + 8 <= w && (w & 7) == 0)  // rows start 16-byte aligned only when w % 8 == 0
-                *reinterpret_cast<uint4*>(dst) = *reinterpret_cast<uint4*>(v);
-            else
-                for (int j = 0; j < 8 && x + j < w; j++) dst[j] = v[j];
-        }
-    }
-}
-
-}  // namespace
-
-extern "C" cudaError_t rfk_unet_to_chw(const void* in, int n_img, int h, int w, int cstride, int coff, int c, int dx,
-                                       void* out, cudaStream_t s) {
-    return rfk_unet_to_chw3(in, n_img, h, w, cstride, coff, c, dx, 1, out, nullptr, nullptr, s);
-}
-
-extern "C" cudaError_t rfk_unet_to_chw3(const void* in, int n_img, int h, int w, int cstride, int coff, int c, int dx0,
-                                        int nshift, void* out0, void* out1, void* out2, cudaStream_t s) {
-    if (n_img <= 0 || h <= 0 || w <= 0 || c <= 0 || c % 8 || cstride % 8 || coff % 8 || nshift < 1 || nshift > 3)
-        return cudaErrorInvalidValue;
-    const void* ptrs[4] = {in, out0, out1, out2};
-    for (const void* p : ptrs)
-        if (reinterpret_cast<size_t>(p) & 15) return cudaErrorMisalignedAddress;
-    dim3 grid((unsigned)((w + 63) / 64), (unsigned)(n_img * h), (unsigned)((c + 31) / 32));
-    to_chw_kernel<<<grid, 256, 0, s>>>(static_cast<const bf16*>(in), h, w, cstride, coff, c, dx0, nshift,
-                                       static_cast<bf16*>(out0), static_cast<bf16*>(out1), static_cast<bf16*>(out2));
-    return cudaGetLastError();
-}
-
-// ------------------------------------------------------------- the rest ----
-namespace {
-
 __device__ __forceinline__ float bf(const bf16 v) { return __bfloat162float(v); }
 
 // Denoiser input of one histogram: 32 bf16 channels per pixel,

@@ -24,9 +24,6 @@ def _L():
     L.rfk_unet_wgrad3x3.restype = C.c_int
     L.rfk_unet_wgrad3x3.argtypes = [C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int,
                                     C.c_int, C.c_void_p, C.c_void_p, C.c_void_p]
-    L.rfk_unet_to_chw.restype = C.c_int
-    L.rfk_unet_to_chw.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_void_p,
-                                  C.c_void_p]
     return L
 
 
