@@ -65,8 +65,10 @@ struct conv_args {
 // starts dx pixel lines later. MODE 2 (all taps): a K block covers all nine
 // taps of one input channel block; its A box holds the tile's R rows plus the
 // row above and below (R + 2 rows of 136 pixels) and the MMAs of tap (dy, dx)
-// start at row r + dy, pixel line dx. The input crosses L2 nine, three or
-// (R + 2) / R times per layer.
+// start at row r + dy, pixel line dx; the layer's weights (up to three input
+// channel blocks x nine taps, one output tile) are loaded once per CTA and
+// stay in shared memory, so the stages carry only the input. The input
+// crosses L2 nine, three or (R + 2) / R times per layer.
 template <int BK, int BN, int MODE>
 struct conv_cfg {
     // R image rows per tile (R accumulators of 128 x BN): small-N layers move
@@ -76,17 +78,20 @@ struct conv_cfg {
     static constexpr int A_ROWS = MODE == 2 ? R + 2 : R;           // image rows per A box
     static constexpr uint32_t A_ROW = (uint32_t)A_PIX * BK * 2u;   // one image row segment
     static constexpr uint32_t A_BYTES = A_ROWS * A_ROW;
-    static constexpr int NB = MODE == 2 ? 9 : (MODE == 1 ? 3 : 1);  // weight tiles per stage
+    static constexpr int NT = MODE == 2 ? 9 : (MODE == 1 ? 3 : 1);  // taps per K block
+    static constexpr int NB = MODE == 2 ? 0 : NT;                    // weight tiles per stage
     static constexpr uint32_t B_TILE = (uint32_t)BN * BK * 2u;
+    static constexpr int KB_RES = 3;                                 // resident input channel blocks (MODE 2)
+    static constexpr uint32_t B_RES = MODE == 2 ? KB_RES * 9u * B_TILE : 0u;
     static constexpr uint32_t LOAD_BYTES = A_BYTES + NB * B_TILE;  // bytes the TMA writes per stage
     static constexpr uint32_t STAGE_BYTES = (LOAD_BYTES + 1023u) & ~1023u;
     static constexpr int TAPS = MODE == 2 ? 1 : (MODE == 1 ? 3 : 9);  // K blocks per input channel block
     // one persistent CTA per SM: as many stages as fit in ~208 KB, at most 8
     static constexpr uint32_t BUDGET = 212992u;
-    static constexpr int STAGES = (BUDGET / STAGE_BYTES > 8) ? 8 : (int)(BUDGET / STAGE_BYTES);
-    static constexpr uint32_t SMEM = STAGES * STAGE_BYTES + 1024u;
+    static constexpr int STAGES = ((BUDGET - B_RES) / STAGE_BYTES > 8) ? 8 : (int)((BUDGET - B_RES) / STAGE_BYTES);
+    static constexpr uint32_t SMEM = B_RES + STAGES * STAGE_BYTES + 1024u;
     static constexpr uint32_t TMEM_COLS = 2u * R * BN;  // two sets of R accumulators
-    static_assert(MODE == 0 || (A_ROW % 512u == 0 && A_BYTES % 1024u == 0 && B_TILE % 1024u == 0),
+    static_assert(MODE == 0 || (A_ROW % 512u == 0 && A_BYTES % 1024u == 0 && B_TILE % 1024u == 0 && B_RES % 1024u == 0),
                   "tap-reuse tiles must stay swizzle-aligned");
     static_assert(STAGES >= 2, "at least two stages");
 };
@@ -135,10 +140,12 @@ __global__ void __launch_bounds__(320, 1) conv3x3_tc(const __grid_constant__ CUt
     using C = conv_cfg<BK, BN, MODE>;
     extern __shared__ uint8_t smem_dyn[];
     uint8_t* base = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_dyn) + 1023) & ~(uintptr_t)1023);
-    __shared__ uint64_t full[C::STAGES], empty[C::STAGES], acc_full[2], acc_empty[2];
+    __shared__ uint64_t full[C::STAGES], empty[C::STAGES], acc_full[2], acc_empty[2], wbar;
     __shared__ uint32_t tmem_base;
     __shared__ int s_fail;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    uint8_t* const res = base;                   // resident weights (MODE 2)
+    uint8_t* const stages = base + C::B_RES;
 
     const int ntn = p.cout / BN;                           // N tiles
     const int rows_t = (p.h + C::R - 1) / C::R;            // row groups per image
@@ -156,6 +163,7 @@ __global__ void __launch_bounds__(320, 1) conv3x3_tc(const __grid_constant__ CUt
             tc::mbar_init(&acc_full[b], 1);
             tc::mbar_init(&acc_empty[b], kEpiWarps);  // one arrival per epilogue warp
         }
+        tc::mbar_init(&wbar, 1);
         s_fail = 0;
         tc::mbar_fence_init();
     }
@@ -169,6 +177,14 @@ __global__ void __launch_bounds__(320, 1) conv3x3_tc(const __grid_constant__ CUt
             // producer: the stage ring runs across tiles
             uint32_t g = 0;
             bool ok = true;
+            if (MODE == 2) {
+                // the layer's weights (one output tile: cout == BN), all taps and input blocks
+                tc::mbar_expect_tx(&wbar, (uint32_t)kpt * 9u * C::B_TILE);
+                for (int cb = 0; cb < kpt; cb++)
+#pragma unroll
+                    for (int t9 = 0; t9 < 9; t9++)
+                        tc::tma_load_2d(res + (cb * 9 + t9) * C::B_TILE, &tmB, &wbar, t9 * p.cin + cb * BK, 0);
+            }
             for (int t = blockIdx.x; ok && t < ntiles; t += gridDim.x) {
                 const int mt = t / ntn, n0 = (t - mt * ntn) * BN;
                 const int xt = mt % p.tiles_x;
@@ -181,14 +197,11 @@ __global__ void __launch_bounds__(320, 1) conv3x3_tc(const __grid_constant__ CUt
                         break;
                     }
                     const int tap = kb / kpt, cb = kb - tap * kpt;
-                    uint8_t* sa = base + (size_t)s * C::STAGE_BYTES;
+                    uint8_t* sa = stages + (size_t)s * C::STAGE_BYTES;
                     tc::mbar_expect_tx(&full[s], C::LOAD_BYTES);
                     if (MODE == 2) {
-                        // rows y - 1 .. y + R, pixels x0 - 1 .. x0 + 134, all nine taps' weights
+                        // rows y - 1 .. y + R, pixels x0 - 1 .. x0 + 134 (weights resident)
                         tc::tma_load_4d(sa, &tmA, &full[s], p.cin_off + cb * BK, xt * 128 - 1, y - 1, img);
-#pragma unroll
-                        for (int t9 = 0; t9 < 9; t9++)
-                            tc::tma_load_2d(sa + C::A_BYTES + t9 * C::B_TILE, &tmB, &full[s], t9 * p.cin + cb * BK, n0);
                     } else if (MODE == 1) {
                         // tap = dy row: pixels x0 - 1 .. x0 + 134, the three column taps' weights
                         tc::tma_load_4d(sa, &tmA, &full[s], p.cin_off + cb * BK, xt * 128 - 1, y + tap - 1, img);
@@ -209,12 +222,14 @@ __global__ void __launch_bounds__(320, 1) conv3x3_tc(const __grid_constant__ CUt
                 for (uint32_t q = g >= (uint32_t)C::STAGES ? g - C::STAGES : 0; q < g; q++)
                     tc::mbar_wait(&full[q % C::STAGES], (q / C::STAGES) & 1);
             }
+            if (MODE == 2 && !tc::mbar_wait(&wbar, 0)) atomicExch(&s_fail, 1);
         }
     } else if (warp == kEpiWarps + 1) {
         if (lane == 0) {
             constexpr uint32_t idesc = tc::idesc_bf16(128, BN);
             uint32_t g = 0;
-            bool ok = true;
+            bool ok = MODE != 2 || tc::mbar_wait(&wbar, 0);
+            const uint32_t sres = tc::smem_u32(res);
             int i = 0;
             for (int t = blockIdx.x; ok && t < ntiles; t += gridDim.x, i++) {
                 const int b = i & 1;
@@ -231,11 +246,13 @@ __global__ void __launch_bounds__(320, 1) conv3x3_tc(const __grid_constant__ CUt
                         break;
                     }
                     tc::fence_after();
-                    const uint32_t sa = tc::smem_u32(base + (size_t)s * C::STAGE_BYTES), sb = sa + C::A_BYTES;
+                    const uint32_t sa = tc::smem_u32(stages + (size_t)s * C::STAGE_BYTES);
+                    // MODE 2: the resident weights of input block kb, else the stage's
+                    const uint32_t sb = MODE == 2 ? sres + (uint32_t)(kb * 9) * C::B_TILE : sa + C::A_BYTES;
 #pragma unroll
                     for (int r = 0; r < C::R; r++)
 #pragma unroll
-                        for (int t = 0; t < C::NB; t++) {
+                        for (int t = 0; t < C::NT; t++) {
                             // MODE 2: tap t = (dy, dx) reads row r + dy; MODE 1: t = dx
                             const int dy = MODE == 2 ? t / 3 : 0, dx = MODE == 2 ? t % 3 : t;
 #pragma unroll
@@ -596,7 +613,8 @@ extern "C" cudaError_t rfk_unet_conv3x3(const void* in, int n_img, int h, int w,
     // block once for all nine taps (MODE 2, 32-channel K blocks so that three
     // 70 KB stages fit); 64 (2 rows) once per tap row (MODE 1); wider tiles
     // (1 row) once per tap (MODE 0)
-    const int mode = bn == 32 ? 2 : (bn == 64 ? 1 : 0);
+    // MODE 2 keeps one output tile's weights resident: cout == 32, at most 3 input blocks
+    const int mode = (bn == 32 && cout == 32 && cin <= 32 * 3) ? 2 : (bn <= 64 ? 1 : 0);
     const int bk = (mode != 2 && cin % 64 == 0 && in_coff % 64 == 0) ? 64 : 32;
     CUtensorMap ma, mb;
     const CUtensorMapSwizzle sw = bk == 64 ? CU_TENSOR_MAP_SWIZZLE_128B : CU_TENSOR_MAP_SWIZZLE_64B;
@@ -637,14 +655,15 @@ extern "C" cudaError_t rfk_unet_conv3x3(const void* in, int n_img, int h, int w,
         switch (bn) {
         case 256: return launch_conv<64, 256, 0>(ma, mb, p, s);
         case 128: return launch_conv<64, 128, 0>(ma, mb, p, s);
-        default: return launch_conv<64, 64, 1>(ma, mb, p, s);
+        case 64: return launch_conv<64, 64, 1>(ma, mb, p, s);
+        default: return launch_conv<64, 32, 1>(ma, mb, p, s);
         }
     }
     switch (bn) {
     case 256: return launch_conv<32, 256, 0>(ma, mb, p, s);
     case 128: return launch_conv<32, 128, 0>(ma, mb, p, s);
     case 64: return launch_conv<32, 64, 1>(ma, mb, p, s);
-    default: return launch_conv<32, 32, 2>(ma, mb, p, s);
+    default: return mode == 2 ? launch_conv<32, 32, 2>(ma, mb, p, s) : launch_conv<32, 32, 1>(ma, mb, p, s);
     }
 }
 
