@@ -249,6 +249,10 @@ __global__ void __launch_bounds__(320, 1) conv3x3_tc(const __grid_constant__ CUt
                     const uint32_t sa = tc::smem_u32(stages + (size_t)s * C::STAGE_BYTES);
                     // MODE 2: the resident weights of input block kb, else the stage's
                     const uint32_t sb = MODE == 2 ? sres + (uint32_t)(kb * 9) * C::B_TILE : sa + C::A_BYTES;
+                    // descriptors of the stage's first tiles; the others differ only in the
+                    // start address field (bits 0-13, 16-byte units; shared memory < 256 KB,
+                    // so adding the compile-time offset cannot carry out of it)
+                    const uint64_t a0 = tc::smem_desc_at(sa, BK * 2), b0 = tc::smem_desc(sb, BK * 2);
 #pragma unroll
                     for (int r = 0; r < C::R; r++)
 #pragma unroll
@@ -258,8 +262,8 @@ __global__ void __launch_bounds__(320, 1) conv3x3_tc(const __grid_constant__ CUt
 #pragma unroll
                             for (int kk = 0; kk < BK / 16; kk++)
                                 tc::mma_bf16(acc + (uint32_t)(r * BN),
-                                             tc::smem_desc_at(sa + (r + dy) * C::A_ROW + dx * (BK * 2) + kk * 32, BK * 2),
-                                             tc::smem_desc(sb + t * C::B_TILE + kk * 32, BK * 2), idesc,
+                                             a0 + (uint64_t)(((r + dy) * C::A_ROW + dx * (BK * 2) + kk * 32) >> 4),
+                                             b0 + (uint64_t)((t * C::B_TILE + kk * 32) >> 4), idesc,
                                              (kb | t | kk) != 0 ? 1u : 0u);
                         }
                     tc::mma_commit(&empty[s]);
