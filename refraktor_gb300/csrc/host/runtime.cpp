@@ -901,8 +901,8 @@ rfk_status rfk_autotune(const rfk_db* db, const rfk_flame* f, const double* samp
             }
         }
         struct cand { int block, cpt, flush, sort, minb; };
-        const cand cands[] = {{256, 4, 1, 2, 5}, {256, 2, 1, 2, 6}, {256, 8, 1, 2, 4}, {256, 4, 2, 2, 5},
-                              {512, 2, 1, 2, 3}, {128, 4, 1, 2, 12}, {256, 4, 0, 2, 5}, {256, 4, 1, 1, 5}};
+        const cand cands[] = {{128, 8, 1, 2, 8}, {256, 8, 1, 2, 4}, {256, 4, 1, 2, 4}, {256, 2, 1, 2, 6},
+                              {128, 4, 1, 2, 12}, {256, 4, 2, 2, 5}, {256, 4, 0, 2, 5}, {256, 4, 1, 1, 5}};
         double best_rate = -1.0, worst_rate = 1e300;
         int n = 0;
         for (const cand& c : cands) {
