@@ -39,6 +39,7 @@ sys.path.insert(0, str(ROOT))
 W, H, SPP = 1920, 1080, 1024.0
 WARMUP_PASSES = 20
 METRIC = "iterations/s"
+DATA = "synthetic (seeded genome refraktor_gb300/workloads/hd_1080p.json)"
 WORKLOAD = "plain 1080p single flame: 1920x1080, 1024 spp, 8 xforms + final xform, 14-variation set, DE blur, tonemap"
 
 
@@ -232,7 +233,7 @@ def run_gpu(args) -> dict:
         "scaling": "weak",
         "vs_baseline": None,
         "dtype": "f32",
-        "data": "synthetic (seeded genome refraktor_gb300/workloads/hd_1080p.json)",
+        "data": DATA,
         "config": {"workload": WORKLOAD, "genome": genome.get("name"), "width": W, "height": H, "spp": SPP, "xforms": 8,
                    "final_xform": True, "grid": info["grid"], "block": info["block"],
                    "chains_per_thread": info["chains_per_thread"], "flush": info["flush"], "sort": info["sort"],
@@ -492,8 +493,9 @@ def run_reference(args) -> dict:
         "metric": METRIC, "value": v, "unit": "iterations/s", "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": 1e3 * total_s / max(args.steps, 1),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-        "data": "synthetic (seeded genome synthetic.hd_flame(0))",
-        "config": {"workload": WORKLOAD, "width": W, "height": H, "spp": SPP},
+        "data": DATA,
+        "config": {"workload": WORKLOAD, "genome": genome.get("name"), "width": W, "height": H, "spp": SPP,
+                   "xforms": 8, "final_xform": True, "parallelism": f"rank 0 of {ws}"},
         "impl": "reference",
         "cpu_baseline": {"value": v, "unit": "iterations/s", "cores": vals[0]["cores"], "kind": "port",
                          "sample": vals[0]["sample"]},
