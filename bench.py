@@ -46,6 +46,12 @@ WORKLOAD = "plain 1080p single flame: 1920x1080, 1024 spp, 8 xforms + final xfor
 # dram__bytes_read.sum + dram__bytes_write.sum of one 1024-spp rfk_bin launch of
 # this workload (ncu, one pass; profiles/rfk_bin_1080p_launch_list.md)
 BIN_DRAM_BYTES_PER_LAUNCH = 39.30e6 + 40.45e3
+# smsp__inst_executed.sum / chain steps of one 16-spp rfk_bin launch of this
+# workload at the bench's launch shape (608 x 256, 8 chains per thread, flush
+# 1, block sort): 451.1 M warp instructions for 36.77 M chain steps (ncu;
+# profiles/rfk_bin_1080p_pipes.md); each SM sub-partition issues one warp
+# instruction per clock
+BIN_WARP_INST_PER_ITER = 451.10e6 / 36.77e6
 
 def _dist():
     ws = int(os.environ.get("WORLD_SIZE", "1"))
@@ -194,6 +200,28 @@ def run_gpu(args) -> dict:
     peak_ops = lr.probe_red_v4(W * H * 16, 512)
     achieved_ops = draws / max(elapsed_kernel, 1e-9) if ws == 1 else draws / t_total
     info = k.info
+    # the chain step's arithmetic pipes: measured SFU and FP32 FMA issue rates
+    # against the translator's per-step counts (weighted by xform weights)
+    per_rank = value / ws
+    pipes = {}
+    for name, pipe, iters, per_iter in (("sfu", 1, 4096, info["sfu_per_iter"]), ("fma", 0, 16384, info["fma_per_iter"])):
+        peak = lr.probe_pipe(pipe, iters)
+        pipes[name] = {"per_iter": per_iter, "achieved_ops": per_rank * per_iter, "peak_ops": peak,
+                       "frac": per_rank * per_iter / peak}
+    pipes["issue"] = {"per_iter": BIN_WARP_INST_PER_ITER}
+    pipes["note"] = ("sfu: transcendental calls of the generated variation code per chain step (a call such as "
+                     "atan2 issues several instructions) vs sin.approx/rsqrt.approx lane ops/s; fma: affine FMAs "
+                     "per chain step (4 per vlink + projection) vs FP32 FMA lane ops/s; both peaks measured live; "
+                     "issue: warp instructions per chain step (ncu) vs one per sub-partition per clock")
+
+    # issue slots: warp instructions per chain step (ncu) x iterations/s vs
+    # 4 sub-partitions x SMs x the median SM clock sampled during the timed steps
+    csum = clocks.summary()
+    mhz = csum.get("sm_mhz") or csum.get("sm_max_mhz") or 2070.0
+    iss = pipes["issue"]
+    iss["achieved_ops"] = per_rank * BIN_WARP_INST_PER_ITER
+    iss["peak_ops"] = 4.0 * lr.sm_count() * mhz * 1e6
+    iss["frac"] = iss["achieved_ops"] / iss["peak_ops"]
 
     # ---- e2e: public API, host samples in, host image out ------------------
     out_host = torch.empty((H, W, 4), dtype=torch.float16, pin_memory=True)
@@ -246,9 +274,10 @@ def run_gpu(args) -> dict:
                      "achieved_ops": achieved_ops, "peak_ops": peak_ops,
                      "note": "red.global.add.v4.f32 payload (16 B per draw); peak = measured random red.v4 rate into a "
                              "buffer of the histogram's size; traffic = DRAM bytes of one 1024-spp rfk_bin "
-                             "launch from an ncu capture (the histogram stays in L2)"},
+                             "launch from an ncu capture (the histogram stays in L2)",
+                     "pipes": pipes},
         "gpu_launches": args.steps * 3,
-        "clocks": clocks.summary(),
+        "clocks": csum,
         "draws_per_s": draws / t_total,
         "bin_ms": 1e3 * bin_launch_s,
         "registers": info["registers"],

@@ -109,6 +109,7 @@ typedef struct {
     size_t sample_floats;   /* floats per prepared parameter block */
     double compile_ms;
     double sfu_per_iter;    /* weighted transcendental calls per chain step */
+    double fma_per_iter;    /* weighted affine FMAs per chain step (4 per vlink, + projection) */
 } rfk_kernel_info;
 
 rfk_status rfk_compile(const rfk_db* db, const rfk_flame* f, const rfk_compile_opts* opts, rfk_kernel** out,
@@ -378,6 +379,9 @@ rfk_status rfk_batch_get_info(const rfk_batch* b, rfk_batch_info* info);
 /* red.global.add.v4.f32 operations per second into a device buffer of
  * `bytes` (random slots): the L2-atomic roofline. */
 rfk_status rfk_probe_red_v4(size_t bytes, uint32_t iters_per_thread, double* ops_per_s);
+/* Issue rate of one arithmetic pipe, in lane operations per second: pipe 0 =
+ * FP32 FMA, pipe 1 = special-function unit (sin.approx / rsqrt.approx). */
+rfk_status rfk_probe_pipe(int pipe, uint32_t iters_per_thread, double* ops_per_s);
 /* Number of SMs of the current device. */
 int rfk_device_sm_count(void);
 

@@ -22,7 +22,7 @@ class KernelInfo(C.Structure):
     _fields_ = [("grid", C.c_int), ("block", C.c_int), ("chains_per_thread", C.c_int), ("flush", C.c_int),
                 ("sort", C.c_int), ("registers", C.c_int), ("num_xforms", C.c_int), ("has_final", C.c_int), ("chaos", C.c_int),
                 ("size_reals", C.c_size_t), ("sample_floats", C.c_size_t), ("compile_ms", C.c_double),
-                ("sfu_per_iter", C.c_double)]
+                ("sfu_per_iter", C.c_double), ("fma_per_iter", C.c_double)]
 
 
 class Bailout(C.Structure):
@@ -116,6 +116,7 @@ SIGNATURES = {
     "rfk_catmull_coefficients": (C.c_int, [C.c_void_p, C.c_uint32, C.c_uint32, C.c_void_p, C.c_void_p]),
     "rfk_fix_rotation": (C.c_int, [C.c_void_p, C.c_size_t, C.c_size_t, C.c_size_t, C.c_void_p, C.c_size_t]),
     "rfk_probe_red_v4": (C.c_int, [C.c_size_t, C.c_uint32, C.POINTER(C.c_double)]),
+    "rfk_probe_pipe": (C.c_int, [C.c_int, C.c_uint32, C.POINTER(C.c_double)]),
     "rfk_device_sm_count": (C.c_int, []),
     "rfk_autotune": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_size_t, C.c_uint32, C.c_uint32, C.c_uint32,
                                C.POINTER(CompileOpts), C.POINTER(TuneReport)]),

@@ -36,6 +36,7 @@ struct emitter {
             const vlink& vl = xf.vchain[li];
             const size_t aff = off;
             fn << "    { // vlink " << li << "\n";
+            info.affines++;
             fn << "        const R aff_a = P[" << aff << "], aff_d = P[" << aff + 1 << "], aff_b = P[" << aff + 2
                << "], aff_e = P[" << aff + 3 << "], aff_c = P[" << aff + 4 << "], aff_f = P[" << aff + 5 << "];\n";
             fn << "        (void)aff_a; (void)aff_b; (void)aff_c; (void)aff_d; (void)aff_e; (void)aff_f;\n";

@@ -22,6 +22,7 @@ struct xform_info {
     size_t base = 0;          // offset of weight in the packed sample
     int rand_calls = 0;       // upper bound of uniform draws per application
     int sfu_ops = 0;          // transcendental calls per application
+    int affines = 0;          // vlink affines per application
 };
 
 struct generated_flame {

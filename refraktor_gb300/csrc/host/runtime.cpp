@@ -226,6 +226,14 @@ std::shared_ptr<kernel_impl> compile(const rfk::flamedb& db, const rfk::flame& f
         sfu += (wsum > 0 ? f.xforms[i].weight / wsum : 0.0) * k->gen.xforms[i].sfu_ops;
     if (k->gen.has_final) sfu += k->gen.xforms.back().sfu_ops;
     k->sfu_per_iter = sfu;
+    // affine FMAs per chain step: 4 per vlink affine (two per coordinate),
+    // weighted like the transcendentals, plus the final xform's and the
+    // screen projection's
+    double fma = 4.0;
+    for (size_t i = 0; i < f.xforms.size(); i++)
+        fma += (wsum > 0 ? f.xforms[i].weight / wsum : 0.0) * 4.0 * k->gen.xforms[i].affines;
+    if (k->gen.has_final) fma += 4.0 * k->gen.xforms.back().affines;
+    k->fma_per_iter = fma;
     k->compile_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
     return k;
 }
@@ -495,6 +503,7 @@ rfk_status rfk_kernel_get_info(const rfk_kernel* kh, rfk_kernel_info* out) {
         out->sample_floats = k.sample_floats;
         out->compile_ms = k.compile_ms;
         out->sfu_per_iter = k.sfu_per_iter;
+        out->fma_per_iter = k.fma_per_iter;
     });
 }
 
@@ -863,6 +872,29 @@ rfk_status rfk_probe_red_v4(size_t bytes, uint32_t iters, double* ops_per_s) {
         cudaEventDestroy(b);
         cudaFree(buf);
         *ops_per_s = (double)blocks * threads * iters / (ms * 1e-3);
+    });
+}
+
+rfk_status rfk_probe_pipe(int pipe, uint32_t iters, double* ops_per_s) {
+    return guard([&] {
+        if (!ops_per_s || (pipe != 0 && pipe != 1) || iters == 0) fail(RFK_E_INVALID, "bad argument");
+        const unsigned blocks = (unsigned)device_sm_count() * 8, threads = 256;
+        float* buf = nullptr;
+        cuda_check(cudaMalloc(&buf, (size_t)blocks * threads * sizeof(float)), "alloc");
+        cudaEvent_t a, b;
+        cudaEventCreate(&a);
+        cudaEventCreate(&b);
+        cuda_check(rfk_launch_pipe_probe(buf, iters, pipe, blocks, threads, nullptr), "probe");
+        cudaEventRecord(a);
+        cuda_check(rfk_launch_pipe_probe(buf, iters, pipe, blocks, threads, nullptr), "probe");
+        cudaEventRecord(b);
+        cuda_check(cudaEventSynchronize(b), "probe");
+        float ms = 0;
+        cudaEventElapsedTime(&ms, a, b);
+        cudaEventDestroy(a);
+        cudaEventDestroy(b);
+        cudaFree(buf);
+        *ops_per_s = (double)blocks * threads * iters * 8.0 / (ms * 1e-3);
     });
 }
 

@@ -102,6 +102,7 @@ struct kernel_impl {
     size_t sample_floats = 0;
     double compile_ms = 0.0;
     double sfu_per_iter = 0.0;
+    double fma_per_iter = 0.0;
     uint32_t salt = 0;
     ~kernel_impl() {
         if (lib) cudaLibraryUnload(lib);

@@ -162,6 +162,36 @@ __global__ void red_v4_probe_kernel(float4* __restrict__ buf, unsigned long long
     }
 }
 
+// Issue-rate probes of the two arithmetic pipes the chain step leans on:
+// pipe 0 = FP32 FMA (8 independent fmaf chains per thread), pipe 1 = the
+// special-function unit (sin.approx and rsqrt.approx, 8 independent chains:
+// sin(x) stays in [-1, 1] and rsqrt of a positive value converges to 1, so no
+// chain reaches inf or NaN). Each thread stores its sum so that nothing is
+// dead code.
+__global__ void pipe_probe_kernel(float* __restrict__ out, unsigned iters, int pipe) {
+    const unsigned gid = blockIdx.x * blockDim.x + threadIdx.x;
+    float a[8];
+#pragma unroll
+    for (int j = 0; j < 8; j++) a[j] = 0.5f + 0.001f * (float)((gid + j) & 255);
+    if (pipe == 0) {
+        for (unsigned i = 0; i < iters; i++) {
+#pragma unroll
+            for (int j = 0; j < 8; j++) a[j] = fmaf(a[j], 0.9999f, 0.0001f);
+        }
+    } else {
+        for (unsigned i = 0; i < iters; i++) {
+#pragma unroll
+            for (int j = 0; j < 4; j++) asm volatile("sin.approx.ftz.f32 %0, %0;" : "+f"(a[j]));
+#pragma unroll
+            for (int j = 4; j < 8; j++) asm volatile("rsqrt.approx.ftz.f32 %0, %0;" : "+f"(a[j]));
+        }
+    }
+    float sum = 0.0f;
+#pragma unroll
+    for (int j = 0; j < 8; j++) sum += a[j];
+    out[gid] = sum;
+}
+
 // ---------------------------------------------------------------- convert --
 // convert_to<In, Out> of assets/kernels/convert.cu:70-99: half3 / half4 in,
 // uchar3 / uchar4 / float3 / float4 out; a byte is min(v * 255, 255)
@@ -273,6 +303,12 @@ cudaError_t rfk_launch_de_blur(const float4* in, float4* out, unsigned w, unsign
 cudaError_t rfk_launch_red_v4_probe(float4* buf, unsigned long long n, unsigned iters, unsigned blocks, unsigned threads,
                                     cudaStream_t s) {
     red_v4_probe_kernel<<<blocks, threads, 0, s>>>(buf, n, iters, 12345u);
+    return cudaGetLastError();
+}
+
+cudaError_t rfk_launch_pipe_probe(float* out, unsigned iters, int pipe, unsigned blocks, unsigned threads,
+                                  cudaStream_t s) {
+    pipe_probe_kernel<<<blocks, threads, 0, s>>>(out, iters, pipe);
     return cudaGetLastError();
 }
 

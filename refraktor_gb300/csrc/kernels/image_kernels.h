@@ -26,6 +26,9 @@ cudaError_t rfk_launch_de_blur(const float4* in, float4* out, unsigned w, unsign
                                float curve, cudaStream_t s);
 cudaError_t rfk_launch_red_v4_probe(float4* buf, unsigned long long n, unsigned iters, unsigned blocks, unsigned threads,
                                     cudaStream_t s);
+// out: blocks * threads floats.
+cudaError_t rfk_launch_pipe_probe(float* out, unsigned iters, int pipe, unsigned blocks, unsigned threads,
+                                  cudaStream_t s);
 cudaError_t rfk_launch_clear_counters(unsigned long long* c, cudaStream_t s);
 // half3 / half4 image -> float3 (2) / float4 (3) / uchar3 (4) / uchar4 (5).
 cudaError_t rfk_launch_convert(const void* in, int in_channels, void* out, int out_format, unsigned w, unsigned h,

@@ -365,6 +365,13 @@ def probe_red_v4(nbytes: int, iters: int = 256) -> float:
     return out.value
 
 
+def probe_pipe(pipe: int, iters: int = 4096) -> float:
+    """Lane operations per second of one arithmetic pipe (0 = FP32 FMA, 1 = SFU)."""
+    out = C.c_double(0)
+    check(lib().rfk_probe_pipe(pipe, iters, C.byref(out)))
+    return out.value
+
+
 def sm_count() -> int:
     return lib().rfk_device_sm_count()
 

@@ -196,6 +196,12 @@ def test_red_v4_probe_runs():
     assert ops > 1e9
 
 
+def test_pipe_probes_run():
+    fma = lr.probe_pipe(0, 4096)
+    sfu = lr.probe_pipe(1, 1024)
+    assert 1e11 < sfu < fma  # the special-function unit has fewer lanes than the FMA pipe
+
+
 def _convert_ref(img, cout, as_bytes, flip_y, swap):
     """numpy restatement of convert_to (assets/kernels/convert.cu:48-99)."""
     v = img.astype(np.float64)

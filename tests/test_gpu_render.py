@@ -37,6 +37,8 @@ def test_warmup_and_bin_reach_quality(db, comp):
     g = syn.plain_flame(0)
     f = lr.flame.from_json(db, g)
     k = comp.get_flame_kernel(db, f)
+    assert not k.info["has_final"]
+    assert k.info["fma_per_iter"] == pytest.approx(8.0)  # one vlink affine per xform + the projection
     w, h = 256, 192
     st = k.warmup(f.pack_samples(4, w, h), (w, h), seed=1, count=20)
     r = k.bin(st, lr.bailout_args(iters=0, millis=0, quality=64.0))
