@@ -12,6 +12,7 @@
 #include <chrono>
 #include <cmath>
 #include <cstring>
+#include <exception>
 #include <map>
 #include <memory>
 #include <mutex>
@@ -65,6 +66,32 @@ struct dev_bin_args {
 constexpr int kCounterWords = 6;
 constexpr int kMaxTemporalMultiplier = 32;  // RFK_MAX_TMUL of rfk_iterate.cuh  // quality, passes, start, stop, draws, status|pad
 constexpr uint32_t kMaxBinMillis = 60000;  // upper bound of one bin call
+
+// Device buffers and events of one call, released on every exit path,
+// including a failed check that throws.
+struct call_scope {
+    std::vector<void*> bufs;
+    std::vector<cudaEvent_t> events;
+    template <class T>
+    T* alloc(size_t bytes, const char* what) {
+        void* p = nullptr;
+        cuda_check(cudaMalloc(&p, bytes), what);
+        bufs.push_back(p);
+        return static_cast<T*>(p);
+    }
+    cudaEvent_t event() {
+        cudaEvent_t e = nullptr;
+        cuda_check(cudaEventCreate(&e), "event");
+        events.push_back(e);
+        return e;
+    }
+    ~call_scope() {
+        // on a failed check a launch of this call may still be reading them
+        if (std::uncaught_exceptions() > 0) cudaDeviceSynchronize();
+        for (void* p : bufs) cudaFree(p);
+        for (cudaEvent_t e : events) cudaEventDestroy(e);
+    }
+};
 
 }  // namespace
 
@@ -689,10 +716,10 @@ rfk_status rfk_apply_xform(const rfk_kernel* kh, const float* params, int xform,
             fail(RFK_E_INVALID, "bad xform index");
         if (n == 0) return;
         if (n > (1u << 30)) fail(RFK_E_INVALID, "too many points");
-        float *dp = nullptr, *di = nullptr, *dout = nullptr;
-        cuda_check(cudaMalloc(&dp, k.sample_floats * 4), "alloc");
-        cuda_check(cudaMalloc(&di, n * 12), "alloc");
-        cuda_check(cudaMalloc(&dout, n * 16), "alloc");
+        call_scope cs;
+        float* dp = cs.alloc<float>(k.sample_floats * 4, "alloc");
+        float* di = cs.alloc<float>(n * 12, "alloc");
+        float* dout = cs.alloc<float>(n * 16, "alloc");
         cuda_check(cudaMemcpy(dp, params, k.sample_floats * 4, cudaMemcpyHostToDevice), "H2D");
         cuda_check(cudaMemcpy(di, in_xyc, n * 12, cudaMemcpyHostToDevice), "H2D");
         unsigned nn = (unsigned)n, sd = seed;
@@ -700,9 +727,6 @@ rfk_status rfk_apply_xform(const rfk_kernel* kh, const float* params, int xform,
         void* args[] = {&dp, &xf, &di, &dout, &nn, &sd};
         launch(k.f_apply, (unsigned)((n + 255) / 256), 256, nullptr, args, "rfk_apply");
         cuda_check(cudaMemcpy(out_xyco, dout, n * 16, cudaMemcpyDeviceToHost), "D2H");
-        cudaFree(dp);
-        cudaFree(di);
-        cudaFree(dout);
     });
 }
 
@@ -714,11 +738,10 @@ rfk_status rfk_prepare_samples(const rfk_kernel* kh, const double* samples, size
         if (count == 0) return;
         std::vector<unsigned> sg(seg, seg + count);
         std::vector<float> tt(t, t + count);
-        float* d = nullptr;
-        cuda_check(cudaMalloc(&d, count * k.sample_floats * 4), "alloc");
+        call_scope cs;
+        float* d = cs.alloc<float>(count * k.sample_floats * 4, "alloc");
         prepare(k, samples, nsamples, sg, tt, seed, d, nullptr);
         cuda_check(cudaMemcpy(out, d, count * k.sample_floats * 4, cudaMemcpyDeviceToHost), "D2H");
-        cudaFree(d);
     });
 }
 
@@ -854,23 +877,18 @@ rfk_status rfk_fix_rotation(double* samples, size_t nsamples, size_t sample_size
 rfk_status rfk_probe_red_v4(size_t bytes, uint32_t iters, double* ops_per_s) {
     return guard([&] {
         if (!ops_per_s || bytes < 16) fail(RFK_E_INVALID, "bad argument");
-        float4* buf = nullptr;
-        cuda_check(cudaMalloc(&buf, bytes), "alloc");
+        call_scope cs;
+        float4* buf = cs.alloc<float4>(bytes, "alloc");
         cuda_check(cudaMemset(buf, 0, bytes), "clear");
         const unsigned blocks = (unsigned)device_sm_count() * 8, threads = 256;
-        cudaEvent_t a, b;
-        cudaEventCreate(&a);
-        cudaEventCreate(&b);
+        cudaEvent_t a = cs.event(), b = cs.event();
         cuda_check(rfk_launch_red_v4_probe(buf, bytes / 16, iters, blocks, threads, nullptr), "probe");
         cudaEventRecord(a);
         cuda_check(rfk_launch_red_v4_probe(buf, bytes / 16, iters, blocks, threads, nullptr), "probe");
         cudaEventRecord(b);
         cuda_check(cudaEventSynchronize(b), "probe");
         float ms = 0;
-        cudaEventElapsedTime(&ms, a, b);
-        cudaEventDestroy(a);
-        cudaEventDestroy(b);
-        cudaFree(buf);
+        cuda_check(cudaEventElapsedTime(&ms, a, b), "probe timing");
         *ops_per_s = (double)blocks * threads * iters / (ms * 1e-3);
     });
 }
@@ -879,21 +897,16 @@ rfk_status rfk_probe_pipe(int pipe, uint32_t iters, double* ops_per_s) {
     return guard([&] {
         if (!ops_per_s || (pipe != 0 && pipe != 1) || iters == 0) fail(RFK_E_INVALID, "bad argument");
         const unsigned blocks = (unsigned)device_sm_count() * 8, threads = 256;
-        float* buf = nullptr;
-        cuda_check(cudaMalloc(&buf, (size_t)blocks * threads * sizeof(float)), "alloc");
-        cudaEvent_t a, b;
-        cudaEventCreate(&a);
-        cudaEventCreate(&b);
+        call_scope cs;
+        float* buf = cs.alloc<float>((size_t)blocks * threads * sizeof(float), "alloc");
+        cudaEvent_t a = cs.event(), b = cs.event();
         cuda_check(rfk_launch_pipe_probe(buf, iters, pipe, blocks, threads, nullptr), "probe");
         cudaEventRecord(a);
         cuda_check(rfk_launch_pipe_probe(buf, iters, pipe, blocks, threads, nullptr), "probe");
         cudaEventRecord(b);
         cuda_check(cudaEventSynchronize(b), "probe");
         float ms = 0;
-        cudaEventElapsedTime(&ms, a, b);
-        cudaEventDestroy(a);
-        cudaEventDestroy(b);
-        cudaFree(buf);
+        cuda_check(cudaEventElapsedTime(&ms, a, b), "probe timing");
         *ops_per_s = (double)blocks * threads * iters * 8.0 / (ms * 1e-3);
     });
 }
