@@ -69,7 +69,7 @@ def test_argument_errors_are_reported(kernel):
         k.warmup(samples, (16, 0), seed=1, count=1)
     with pytest.raises(lr.RfkError):
         k.warmup(samples, (1 << 16, 1 << 16), seed=1, count=1)  # 2^32 pixels: beyond the 2^31 limit
-    ss =k.info["size_reals"] + 768
+    ss = k.info["size_reals"] + 768
     with pytest.raises(lr.RfkError):
         k.warmup(samples[: 3 * ss], (16, 16), seed=1, count=1)  # fewer than four samples
     with pytest.raises(lr.RfkError):
