@@ -1,4 +1,4 @@
-"""Benchmark of the flame-rendering hot path (see the design doc for the contract).
+"""Benchmark of the flame-rendering hot path.
 
 Workload: the plain 1080p single flame - 1920x1080, 1024 spp, 8 xforms with
 Dirichlet(1) weights plus a final xform, 1-3 variations each from the

@@ -33,11 +33,15 @@ from __future__ import annotations
 
 import ctypes as C
 import json
+import os
 import sys
 from pathlib import Path
 
 HERE = Path(__file__).resolve().parent
 OUT = HERE / "_ref"
+# the reference checkout this recipe reads (absent on machines that only run
+# the prebuilt files); RFK_REFERENCE_ROOT overrides it
+REFERENCE_ROOT = Path(os.environ.get("RFK_REFERENCE_ROOT", "/root/reference"))
 CUDA = Path("/usr/local/cuda")
 
 MODULES = {
@@ -163,4 +167,4 @@ def build(ref_root: Path) -> None:
 
 
 if __name__ == "__main__":
-    build(Path(sys.argv[1] if len(sys.argv) > 1 else "/root/reference"))
+    build(Path(sys.argv[1]) if len(sys.argv) > 1 else REFERENCE_ROOT)

@@ -6,7 +6,7 @@ import pytest
 ROOT = Path(__file__).resolve().parent.parent
 sys.path.insert(0, str(ROOT))
 
-REFERENCE = Path("/root/reference")
+from oracle.build_ref import REFERENCE_ROOT as REFERENCE  # noqa: E402
 
 
 def pytest_configure(config):

@@ -11,6 +11,7 @@ from pathlib import Path
 import numpy as np
 import pytest
 
+from oracle.build_ref import REFERENCE_ROOT as REFERENCE
 from refraktor_gb300 import librefrakt as lr
 from refraktor_gb300 import synthetic as syn
 from refraktor_gb300 import _lib
@@ -215,7 +216,7 @@ def test_flam3_import(db):
 
 
 def test_flam3_reference_fixture(db):
-    p = Path("/root/reference/assets/flames_test/electricsheep.247.50049.flam3")
+    p = REFERENCE / "assets/flames_test/electricsheep.247.50049.flam3"
     if not p.exists():
         pytest.skip("reference fixture not present")
     f = lr.flame.import_flam3(db, p.read_text())
