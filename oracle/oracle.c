@@ -1,6 +1,6 @@
 /*
  * FP64 CPU oracle of the flame-rendering hot path. TEST INFRASTRUCTURE ONLY
- * (see oracle.h): the checker for librfk's CUDA kernels, and the timed CPU
+ * (see oracle.h): the oracle librfk's CUDA kernels are tested against, and the timed CPU
  * baseline. Not part of the library.
  */
 #include "oracle.h"

@@ -1,7 +1,7 @@
 /*
  * FP64 CPU oracle of the flame-rendering hot path. TEST INFRASTRUCTURE ONLY:
  * used by tests/, __graft_entry__.smoke() and bench.py's cpu_baseline /
- * reference legs as the checker; never linked into or called by librfk.
+ * reference legs as the oracle; never linked into or called by librfk.
  *
  * It restates the reference's formulas independently of the library (no
  * shared source): packed-sample interpolation, the chaos game, the tonemap,

@@ -1,5 +1,5 @@
 """Python side of the FP64 CPU oracle. TEST INFRASTRUCTURE ONLY: imported by
-tests/, __graft_entry__.smoke() and bench.py's CPU legs as the checker; the
+tests/, __graft_entry__.smoke() and bench.py's CPU legs as the oracle; the
 library never uses it.
 
 Restates from the reference (paths relative to its root):
