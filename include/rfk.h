@@ -140,6 +140,16 @@ rfk_status rfk_kernel_source(const rfk_kernel* k, char* buf, size_t cap, size_t*
  * count), each (block, sample) reaching an equal share of the quality. */
 rfk_status rfk_warmup(const rfk_kernel* k, const double* samples, size_t nsamples, uint32_t w, uint32_t h,
                       uint32_t seed, uint32_t warmup_count, int temporal_multiplier, void* stream, rfk_state** out);
+/* flame_kernel::warmup(stream, samples, gpu_image<float4>&& bins, seed, count,
+ * temporal_multiplier)  flame_compiler.h:100, flame_compiler.cpp:1037-1101
+ * As rfk_warmup, but the state accumulates into the caller's w x h float4
+ * histogram `bins` (device, 16-byte aligned) as it is, without clearing it
+ * (the reference adopts the image it is given; its dims overload clears a new
+ * one). The caller keeps ownership: `bins` must outlive the state and is not
+ * freed by rfk_state_destroy. */
+rfk_status rfk_warmup_adopt(const rfk_kernel* k, const double* samples, size_t nsamples, void* bins, uint32_t w,
+                            uint32_t h, uint32_t seed, uint32_t warmup_count, int temporal_multiplier, void* stream,
+                            rfk_state** out);
 void rfk_state_destroy(rfk_state* s);
 
 /* flame_kernel::bailout_args  flame_compiler.h:92-96 */

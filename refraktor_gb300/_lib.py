@@ -95,6 +95,8 @@ SIGNATURES = {
     "rfk_kernel_source": (C.c_int, [C.c_void_p, C.c_char_p, C.c_size_t, c_size_p]),
     "rfk_warmup": (C.c_int, [C.c_void_p, C.POINTER(C.c_double), C.c_size_t, C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint32,
                              C.c_int, C.c_void_p, C.POINTER(C.c_void_p)]),
+    "rfk_warmup_adopt": (C.c_int, [C.c_void_p, C.POINTER(C.c_double), C.c_size_t, C.c_void_p, C.c_uint32, C.c_uint32,
+                                   C.c_uint32, C.c_uint32, C.c_int, C.c_void_p, C.POINTER(C.c_void_p)]),
     "rfk_state_destroy": (None, [C.c_void_p]),
     "rfk_bin": (C.c_int, [C.c_void_p, C.POINTER(Bailout), C.c_void_p, C.POINTER(BinResult)]),
     "rfk_bin_async": (C.c_int, [C.c_void_p, C.POINTER(Bailout), C.c_void_p]),

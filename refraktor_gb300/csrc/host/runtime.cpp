@@ -110,14 +110,16 @@ struct rfk_state {
     unsigned* h_stop = nullptr;                // mapped pinned
     unsigned* d_stop = nullptr;
     cudaEvent_t done = nullptr;
+    bool own_bins = true;  // false: the caller's histogram (rfk_warmup_adopt)
     unsigned call_id = 0;
     double quality = 0.0;
     bool pending = false;
 
     ~rfk_state() {
         if (done) cudaEventSynchronize(done);
-        for (void* p : {(void*)d_samples, (void*)d_x, (void*)d_y, (void*)d_c, (void*)d_last, (void*)d_bins, (void*)d_counters})
+        for (void* p : {(void*)d_samples, (void*)d_x, (void*)d_y, (void*)d_c, (void*)d_last, (void*)d_counters})
             if (p) cudaFree(p);
+        if (d_bins && own_bins) cudaFree(d_bins);
         if (h_counters) cudaFreeHost(h_counters);
         if (h_stop) cudaFreeHost(h_stop);
         if (done) cudaEventDestroy(done);
@@ -538,11 +540,17 @@ rfk_status rfk_kernel_source(const rfk_kernel* kh, char* buf, size_t cap, size_t
     return guard([&] { copy_out(buf, cap, len, K(kh).gen.source); });
 }
 
-rfk_status rfk_warmup(const rfk_kernel* kh, const double* samples, size_t nsamples, uint32_t w, uint32_t h, uint32_t seed,
-                      uint32_t warmup_count, int temporal_multiplier, void* stream, rfk_state** out) {
+namespace {
+// Both warm-up entry points: a fresh cleared histogram (adopt == nullptr), or
+// the caller's histogram taken as it is (flame_compiler.cpp:1037-1101 does
+// not clear an adopted image; the dims overload at :1103-1108 clears its own).
+rfk_status warmup_impl(const rfk_kernel* kh, const double* samples, size_t nsamples, float4* adopt, uint32_t w,
+                       uint32_t h, uint32_t seed, uint32_t warmup_count, int temporal_multiplier, void* stream,
+                       rfk_state** out) {
     return guard([&] {
         auto k = Kshared(kh);
         if (!samples || !out) fail(RFK_E_INVALID, "null argument");
+        if (adopt && reinterpret_cast<uintptr_t>(adopt) % 16 != 0) fail(RFK_E_INVALID, "histogram must be 16-byte aligned");
         if (w == 0 || h == 0) fail(RFK_E_INVALID, "image size must be positive");
         if ((uint64_t)w * h > (1ull << 31)) fail(RFK_E_INVALID, "image too large");
         if (temporal_multiplier < 1 || temporal_multiplier > kMaxTemporalMultiplier)
@@ -568,8 +576,13 @@ rfk_status rfk_warmup(const rfk_kernel* kh, const double* samples, size_t nsampl
         cuda_check(cudaMalloc(&st->d_c, st->nchains * sizeof(float)), "alloc chains");
         cuda_check(cudaMalloc(&st->d_last, st->nchains), "alloc chains");
         cuda_check(cudaMemsetAsync(st->d_last, 255, st->nchains, s), "init chains");
-        cuda_check(cudaMalloc(&st->d_bins, (size_t)w * h * sizeof(float4)), "alloc histogram");
-        cuda_check(cudaMemsetAsync(st->d_bins, 0, (size_t)w * h * sizeof(float4), s), "clear histogram");
+        if (adopt) {
+            st->d_bins = adopt;
+            st->own_bins = false;
+        } else {
+            cuda_check(cudaMalloc(&st->d_bins, (size_t)w * h * sizeof(float4)), "alloc histogram");
+            cuda_check(cudaMemsetAsync(st->d_bins, 0, (size_t)w * h * sizeof(float4), s), "clear histogram");
+        }
         cuda_check(cudaMalloc(&st->d_counters, (kCounterWords + 98) * sizeof(unsigned long long)), "alloc counters");
         cuda_check(cudaMemsetAsync(st->d_counters, 0, (kCounterWords + 98) * sizeof(unsigned long long), s), "clear counters");
         cuda_check(cudaHostAlloc(&st->h_counters, (kCounterWords + 98) * sizeof(unsigned long long), cudaHostAllocDefault), "pinned");
@@ -584,6 +597,20 @@ rfk_status rfk_warmup(const rfk_kernel* kh, const double* samples, size_t nsampl
         cuda_check(cudaStreamSynchronize(s), "warmup");
         *out = st.release();
     });
+}
+}  // namespace
+
+rfk_status rfk_warmup(const rfk_kernel* kh, const double* samples, size_t nsamples, uint32_t w, uint32_t h, uint32_t seed,
+                      uint32_t warmup_count, int temporal_multiplier, void* stream, rfk_state** out) {
+    return warmup_impl(kh, samples, nsamples, nullptr, w, h, seed, warmup_count, temporal_multiplier, stream, out);
+}
+
+rfk_status rfk_warmup_adopt(const rfk_kernel* kh, const double* samples, size_t nsamples, void* bins, uint32_t w,
+                            uint32_t h, uint32_t seed, uint32_t warmup_count, int temporal_multiplier, void* stream,
+                            rfk_state** out) {
+    if (!bins) return guard([] { fail(RFK_E_INVALID, "null histogram"); });
+    return warmup_impl(kh, samples, nsamples, static_cast<float4*>(bins), w, h, seed, warmup_count,
+                       temporal_multiplier, stream, out);
 }
 
 void rfk_state_destroy(rfk_state* s) { delete s; }

@@ -206,15 +206,31 @@ class flame_kernel:
     def source(self) -> str:
         return text_out(lib().rfk_kernel_source, self._h)
 
-    def warmup(self, samples: np.ndarray, dims: Sequence[int], seed: int, count: int, temporal_multiplier: int = 1,
+    def warmup(self, samples: np.ndarray, dims, seed: int, count: int, temporal_multiplier: int = 1,
                stream=None) -> "saved_state":
-        """flame_kernel::warmup(stream, samples, dims, seed, count, temporal_multiplier)."""
+        """flame_kernel::warmup(stream, samples, dims | bins, seed, count,
+        temporal_multiplier) (flame_compiler.h:99-100). `dims` is (w, h) for
+        a new cleared histogram, or a float32 CUDA tensor (h, w, 4) that the
+        state adopts as it is, without clearing (flame_compiler.cpp:1037);
+        the state keeps a reference to the tensor."""
         s = np.ascontiguousarray(samples, dtype=np.float64)
         ss = self.info["size_reals"] + 768
         if s.size % ss != 0:
             raise RfkError(1, f"samples length {s.size} is not a multiple of the sample size {ss}")
         h = C.c_void_p()
-        check(lib().rfk_warmup(self._h, s.ctypes.data_as(C.POINTER(C.c_double)), s.size // ss, int(dims[0]), int(dims[1]),
+        sp = s.ctypes.data_as(C.POINTER(C.c_double))
+        if hasattr(dims, "data_ptr"):
+            bins = dims
+            if (bins.dim() != 3 or bins.shape[2] != 4 or not bins.is_contiguous() or str(bins.dtype) != "torch.float32"
+                    or not bins.is_cuda):
+                raise RfkError(1, "an adopted histogram is a contiguous (h, w, 4) float32 CUDA tensor")
+            w, hh = int(bins.shape[1]), int(bins.shape[0])
+            check(lib().rfk_warmup_adopt(self._h, sp, s.size // ss, C.c_void_p(bins.data_ptr()), w, hh, seed & 0xFFFFFFFF,
+                                         count, temporal_multiplier, _stream_ptr(stream), C.byref(h)))
+            st = saved_state(h, self, (w, hh))
+            st._adopted = bins
+            return st
+        check(lib().rfk_warmup(self._h, sp, s.size // ss, int(dims[0]), int(dims[1]),
                                seed & 0xFFFFFFFF, count, temporal_multiplier, _stream_ptr(stream), C.byref(h)))
         return saved_state(h, self, (int(dims[0]), int(dims[1])))
 

@@ -101,6 +101,31 @@ def test_deterministic_with_pass_cap(db, comp):
     np.testing.assert_allclose(outs[0], outs[1], rtol=1e-4, atol=1e-6)
 
 
+def test_warmup_adopts_the_callers_histogram(db, comp):
+    """warmup(samples, bins&&, ...) (flame_compiler.cpp:1037-1101): the state
+    draws into the caller's image as it is, without clearing it."""
+    g = syn.plain_flame(4)
+    f = lr.flame.from_json(db, g)
+    k = comp.get_flame_kernel(db, f)
+    w, h = 96, 64
+    samples = f.pack_samples(4, w, h)
+    st = k.warmup(samples, (w, h), seed=9, count=20)
+    r1 = k.bin(st, lr.bailout_args(iters=10, millis=0, quality=0))
+    ref = st.bins().cpu().numpy().astype(np.float64)
+    pre = torch.ones((h, w, 4), dtype=torch.float32, device="cuda")
+    st2 = k.warmup(samples, pre, seed=9, count=20)
+    assert st2.dims == (w, h) and st2.bins().data_ptr() == pre.data_ptr()
+    r2 = k.bin(st2, lr.bailout_args(iters=10, millis=0, quality=0))
+    assert r2.draw_count == r1.draw_count and r2.quality == r1.quality
+    got = pre.cpu().numpy().astype(np.float64)
+    np.testing.assert_array_equal(got[..., 3] - 1.0, ref[..., 3])  # same draws on top of the 1.0 already there
+    np.testing.assert_allclose(got[..., :3] - 1.0, ref[..., :3], rtol=1e-4, atol=1e-5)
+    del st2
+    assert torch.all(pre[..., 3] >= 1.0).item()  # the caller's buffer outlives the state
+    with pytest.raises(lr.RfkError):
+        k.warmup(samples, torch.ones((h, w, 3), dtype=torch.float32, device="cuda"), seed=9, count=1)
+
+
 def test_prepared_flame_matches_oracle_interpolation(db, comp):
     """Row a3/a4: FP32 Catmull-Rom + polar affines + 8-bit palette vs FP64."""
     rng = np.random.default_rng(11)
