@@ -52,6 +52,24 @@ int rfk_db_variation_count(const rfk_db* db);
 rfk_status rfk_db_variation_name(const rfk_db* db, int index, char* buf, size_t cap);
 /* flamedb::hash()  flame_info.h:131-133 */
 uint64_t rfk_db_hash(const rfk_db* db);
+/* flamedb::add_or_update_variation  flame_info.h:94, flame_info.cpp:152-194
+ * Adds or replaces every variation of `yaml` (the variations_new.yml format:
+ * name: body, or name: {src, precalc, param, tags}), in name order; each is
+ * parsed and checked against its parameters and the commons. On the first
+ * failure returns RFK_E_FORMAT (message in rfk_last_error) with the earlier
+ * entries kept. Changes rfk_db_hash, so kernels compiled afterwards see the
+ * new definitions. Not thread-safe against other calls on the same db. */
+rfk_status rfk_db_add_variations(rfk_db* db, const char* yaml);
+/* flamedb::add_or_update_common  flame_info.h:95: a named common expression. */
+rfk_status rfk_db_add_common(rfk_db* db, const char* name, const char* code);
+/* flamedb::remove_variation / remove_common  flame_info.h:113-129:
+ * 1 removed, 0 not present (or a null argument). */
+int rfk_db_remove_variation(rfk_db* db, const char* name);
+int rfk_db_remove_common(rfk_db* db, const char* name);
+/* flamedb::is_variation / is_parameter / is_common  flame_info.h:69-84: 1 or 0. */
+int rfk_db_is_variation(const rfk_db* db, const char* name);
+int rfk_db_is_parameter(const rfk_db* db, const char* variation, const char* param);
+int rfk_db_is_common(const rfk_db* db, const char* name);
 /* Translated device source of one variation (diagnostics, host-twin tests). */
 rfk_status rfk_db_variation_source(const rfk_db* db, const char* name, char* buf, size_t cap, size_t* len);
 

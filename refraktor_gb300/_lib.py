@@ -77,6 +77,13 @@ SIGNATURES = {
     "rfk_db_variation_count": (C.c_int, [C.c_void_p]),
     "rfk_db_variation_name": (C.c_int, [C.c_void_p, C.c_int, C.c_char_p, C.c_size_t]),
     "rfk_db_hash": (C.c_uint64, [C.c_void_p]),
+    "rfk_db_add_variations": (C.c_int, [C.c_void_p, C.c_char_p]),
+    "rfk_db_add_common": (C.c_int, [C.c_void_p, C.c_char_p, C.c_char_p]),
+    "rfk_db_remove_variation": (C.c_int, [C.c_void_p, C.c_char_p]),
+    "rfk_db_remove_common": (C.c_int, [C.c_void_p, C.c_char_p]),
+    "rfk_db_is_variation": (C.c_int, [C.c_void_p, C.c_char_p]),
+    "rfk_db_is_parameter": (C.c_int, [C.c_void_p, C.c_char_p, C.c_char_p]),
+    "rfk_db_is_common": (C.c_int, [C.c_void_p, C.c_char_p]),
     "rfk_db_variation_source": (C.c_int, [C.c_void_p, C.c_char_p, C.c_char_p, C.c_size_t, c_size_p]),
     "rfk_flame_from_json": (C.c_int, [C.c_void_p, C.c_char_p, C.POINTER(C.c_void_p)]),
     "rfk_flame_from_flam3": (C.c_int, [C.c_void_p, C.c_char_p, C.POINTER(C.c_void_p)]),

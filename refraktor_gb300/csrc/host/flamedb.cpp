@@ -105,6 +105,22 @@ bool flamedb::add_or_update_common(const std::string& name, const std::string& s
     return true;
 }
 
+bool flamedb::remove_variation(const std::string& name) {
+    auto it = variations_.find(name);
+    if (it == variations_.end()) return false;
+    if (it->second.pad) pads_[*it->second.pad].erase(name);
+    variations_.erase(it);
+    recalc_hash();
+    return true;
+}
+
+bool flamedb::remove_common(const std::string& name) {
+    if (!commons_.erase(name)) return false;
+    common_ast_.erase(name);
+    recalc_hash();
+    return true;
+}
+
 std::vector<std::string> flamedb::common_closure(const std::set<std::string>& direct) const {
     std::vector<std::string> order;
     std::set<std::string> seen;
@@ -146,12 +162,19 @@ static std::string read_file(const std::string& path) {
 }
 
 void load_flamedb(flamedb& db, const std::string& dir) {
-    value vdefs = parse_yaml(read_file(dir + "/variations_new.yml"));
+    const std::string vtext = read_file(dir + "/variations_new.yml");
     value cdefs = parse_yaml(read_file(dir + "/common.yml"));
     std::string err;
     for (auto& [name, src] : cdefs.obj) {
         if (!db.add_or_update_common(name, src.as_string(), err)) throw format_error(err);
     }
+    add_variations_yaml(db, vtext);
+}
+
+void add_variations_yaml(flamedb& db, const std::string& yaml_text) {
+    value vdefs = parse_yaml(yaml_text);
+    if (!vdefs.is_object()) throw format_error("a variation document is a mapping of names to definitions");
+    std::string err;
     std::vector<std::string> names;
     for (auto& [name, _] : vdefs.obj) names.push_back(name);
     std::sort(names.begin(), names.end());

@@ -52,8 +52,17 @@ public:
     bool add_or_update_variation(const variation_def& def, std::string& err);
     bool add_or_update_common(const std::string& name, const std::string& source, std::string& err);
 
+    // flamedb::remove_variation / remove_common (flame_info.h:113-129): false
+    // when the name is not present
+    bool remove_variation(const std::string& name);
+    bool remove_common(const std::string& name);
+
     bool is_variation(const std::string& n) const { return variations_.count(n) > 0; }
     bool is_common(const std::string& n) const { return commons_.count(n) > 0; }
+    bool is_parameter(const std::string& v, const std::string& p) const {
+        auto it = variations_.find(v);
+        return it != variations_.end() && it->second.params.count(p) > 0;
+    }
     const variation_def& get_variation(const std::string& n) const { return variations_.at(n); }
     const dsl::node& common_ast(const std::string& n) const { return *common_ast_.at(n); }
     const std::map<std::string, variation_def>& variations() const { return variations_; }
@@ -77,6 +86,10 @@ private:
 // Loads `<dir>/variations_new.yml` and `<dir>/common.yml` into `db`
 // (flame_info.cpp:60-148). Throws rfk::format_error on failure.
 void load_flamedb(flamedb& db, const std::string& dir);
+// Adds or replaces the variations of a document in variations_new.yml format
+// (name: body, or name: {src, precalc, param, tags}), in name order; the
+// first failure throws rfk::format_error and leaves the earlier ones added.
+void add_variations_yaml(flamedb& db, const std::string& yaml_text);
 
 uint64_t fnv1a(const std::string& s, uint64_t h = 1469598103934665603ull);
 

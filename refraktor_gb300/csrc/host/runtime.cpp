@@ -378,6 +378,29 @@ rfk_status rfk_db_variation_name(const rfk_db* db, int index, char* buf, size_t 
 
 uint64_t rfk_db_hash(const rfk_db* db) { return db ? db->db.hash() : 0; }
 
+rfk_status rfk_db_add_variations(rfk_db* db, const char* yaml) {
+    return guard([&] {
+        if (!db || !yaml) fail(RFK_E_INVALID, "null argument");
+        rfk::add_variations_yaml(db->db, yaml);
+    });
+}
+
+rfk_status rfk_db_add_common(rfk_db* db, const char* name, const char* code) {
+    return guard([&] {
+        if (!db || !name || !code) fail(RFK_E_INVALID, "null argument");
+        std::string err;
+        if (!db->db.add_or_update_common(name, code, err)) fail(RFK_E_FORMAT, err);
+    });
+}
+
+int rfk_db_remove_variation(rfk_db* db, const char* name) { return db && name && db->db.remove_variation(name) ? 1 : 0; }
+int rfk_db_remove_common(rfk_db* db, const char* name) { return db && name && db->db.remove_common(name) ? 1 : 0; }
+int rfk_db_is_variation(const rfk_db* db, const char* name) { return db && name && db->db.is_variation(name) ? 1 : 0; }
+int rfk_db_is_parameter(const rfk_db* db, const char* v, const char* p) {
+    return db && v && p && db->db.is_parameter(v, p) ? 1 : 0;
+}
+int rfk_db_is_common(const rfk_db* db, const char* name) { return db && name && db->db.is_common(name) ? 1 : 0; }
+
 rfk_status rfk_db_variation_source(const rfk_db* db, const char* name, char* buf, size_t cap, size_t* len) {
     return guard([&] {
         if (!db || !name) fail(RFK_E_INVALID, "null argument");

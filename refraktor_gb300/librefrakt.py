@@ -76,7 +76,27 @@ class flamedb:
         return out
 
     def is_variation(self, name: str) -> bool:
-        return name in self.variations()
+        return lib().rfk_db_is_variation(self._h, name.encode()) == 1
+
+    def is_parameter(self, vname: str, pname: str) -> bool:
+        return lib().rfk_db_is_parameter(self._h, vname.encode(), pname.encode()) == 1
+
+    def is_common(self, name: str) -> bool:
+        return lib().rfk_db_is_common(self._h, name.encode()) == 1
+
+    def add_or_update_variations(self, yaml_text: str) -> None:
+        """flamedb::add_or_update_variation for every entry of a document in
+        variations_new.yml format; raises RfkError on the first invalid one."""
+        check(lib().rfk_db_add_variations(self._h, yaml_text.encode()))
+
+    def add_or_update_common(self, name: str, code: str) -> None:
+        check(lib().rfk_db_add_common(self._h, name.encode(), code.encode()))
+
+    def remove_variation(self, name: str) -> bool:
+        return lib().rfk_db_remove_variation(self._h, name.encode()) == 1
+
+    def remove_common(self, name: str) -> bool:
+        return lib().rfk_db_remove_common(self._h, name.encode()) == 1
 
     def hash(self) -> int:
         return lib().rfk_db_hash(self._h)

@@ -226,3 +226,41 @@ def test_flam3_reference_fixture(db):
     assert len(js["xforms"][1]["vchain"]) == 2  # post affine -> linear vlink
     assert js["gamma"] == 4 and js["brightness"] == pytest.approx(64.0783)
     lr.compile_check(db, f, "sm_103a")
+
+
+def test_db_add_remove_and_queries():
+    """flamedb::add_or_update_variation / add_or_update_common / remove_* /
+    is_* (flame_info.h:69-129) on a private database."""
+    fdb = lr.flamedb()
+    h0 = fdb.hash()
+    assert fdb.is_variation("julian") and fdb.is_parameter("julian", "power") and fdb.is_parameter("julian", "rN")
+    assert not fdb.is_parameter("julian", "nope") and not fdb.is_variation("scaled_linear")
+    assert fdb.is_common("phi") and not fdb.is_common("double_r")
+    fdb.add_or_update_common("double_r", "2.0 * common.sqrt")
+    fdb.add_or_update_variations(
+        "scaled_linear:\n"
+        "  param:\n"
+        "    s: {default: 2.0}\n"
+        "  src: |-\n"
+        "    result += weight * param.s * p;\n"
+        "ring_r: result += weight * common.double_r * p;\n")
+    assert fdb.is_common("double_r") and fdb.is_variation("scaled_linear") and fdb.is_variation("ring_r")
+    assert fdb.is_parameter("scaled_linear", "s")
+    h1 = fdb.hash()
+    assert h1 != h0
+    # a genome can use the new variation, and its generated code reads its parameter
+    g = syn.plain_flame(0)
+    g["xforms"][0]["vchain"][0]["variations"] = {"scaled_linear": {"weight": 0.5, "s": 3.0}}
+    f = lr.flame.from_json(fdb, g)
+    assert f.size_reals() > 0
+    # invalid bodies are rejected and leave the database as it was
+    with pytest.raises(_lib.RfkError) as e:
+        fdb.add_or_update_variations("broken: result += weight * param.missing * p;\n")
+    assert e.value.code == 2 and not fdb.is_variation("broken") and fdb.hash() == h1
+    with pytest.raises(_lib.RfkError):
+        fdb.add_or_update_common("bad", "p.x +")
+    assert fdb.remove_variation("ring_r") and not fdb.remove_variation("ring_r")
+    assert not fdb.is_variation("ring_r") and fdb.hash() != h1
+    assert fdb.remove_common("double_r") and not fdb.is_common("double_r")
+    assert fdb.remove_variation("scaled_linear")
+    assert fdb.hash() == h0  # back to the loaded definitions
