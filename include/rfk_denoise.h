@@ -29,6 +29,12 @@ typedef struct rfk_denoiser rfk_denoiser;
 /* A network with seeded He-initialised weights. */
 rfk_status rfk_denoiser_create(uint64_t seed, rfk_denoiser** out);
 void rfk_denoiser_destroy(rfk_denoiser* d);
+/* Reads the parameters of a weight file written by the Python side
+ * (refraktor_gb300.denoise.denoiser.save: NumPy .npz with a 1-D float16 or
+ * float32 `params` array, e.g. refraktor_gb300/workloads/denoiser_weights.npz)
+ * into host floats in the rfk_denoiser_set_params layout. *count = the number
+ * of parameters; with out == NULL only the count is returned. */
+rfk_status rfk_denoiser_read_params(const char* path, float* out, size_t cap, size_t* count);
 /* Parameters: per layer the f32 weights [cout][9][cin] then the biases [cout] (host arrays). */
 size_t rfk_denoiser_param_count(const rfk_denoiser* d);
 rfk_status rfk_denoiser_get_params(const rfk_denoiser* d, float* out, size_t n);

@@ -149,6 +149,7 @@ SIGNATURES = {
     "rfk_denoiser_param_count": (C.c_size_t, [C.c_void_p]),
     "rfk_denoiser_get_params": (C.c_int, [C.c_void_p, C.c_void_p, C.c_size_t]),
     "rfk_denoiser_set_params": (C.c_int, [C.c_void_p, C.c_void_p, C.c_size_t]),
+    "rfk_denoiser_read_params": (C.c_int, [C.c_char_p, C.c_void_p, C.c_size_t, C.POINTER(C.c_size_t)]),
     "rfk_denoiser_features": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint32, C.c_uint32, C.c_double, C.c_void_p,
                                         C.c_void_p]),
     "rfk_denoiser_train_step": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_uint32, C.c_uint32, C.c_uint32,

@@ -115,7 +115,12 @@ std::vector<uint8_t> zlib_uncompress(const std::vector<uint8_t>& data) {
     uint8_t cmf = data[0], flg = data[1];
     if ((cmf & 0x0F) != 8 || ((cmf << 8) | flg) % 31 != 0) throw format_error("zlib: bad header");
     if (flg & 0x20) throw format_error("zlib: preset dictionary not supported");
-    bit_reader br{data, 2};
+    return inflate_raw(data, 2);
+}
+
+std::vector<uint8_t> inflate_raw(const std::vector<uint8_t>& data, size_t start) {
+    if (start >= data.size()) throw format_error("deflate: stream too short");
+    bit_reader br{data, start};
     std::vector<uint8_t> out;
     int final_block = 0;
     do {

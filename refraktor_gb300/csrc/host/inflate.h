@@ -13,5 +13,8 @@ namespace rfk {
 
 std::vector<uint8_t> base64_decode(const std::string& text);
 std::vector<uint8_t> zlib_uncompress(const std::vector<uint8_t>& data);
+// A raw DEFLATE stream starting at data[start] (self-terminating: its last block
+// is marked), as stored in zip members.
+std::vector<uint8_t> inflate_raw(const std::vector<uint8_t>& data, size_t start);
 
 }  // namespace rfk

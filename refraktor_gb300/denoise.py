@@ -267,5 +267,15 @@ def _profile_case(argv=None) -> None:
     print(f"{a.case}: {e0.elapsed_time(e1) / a.reps:.3f} ms per call")
 
 
+def read_params(path: str | Path) -> np.ndarray:
+    """The parameters of a weight file through the library's own reader
+    (rfk_denoiser_read_params), as a C or C++ caller loads them."""
+    n = C.c_size_t()
+    check(lib().rfk_denoiser_read_params(str(path).encode(), None, 0, C.byref(n)))
+    out = np.empty(n.value, dtype=np.float32)
+    check(lib().rfk_denoiser_read_params(str(path).encode(), out.ctypes.data, out.size, C.byref(n)))
+    return out
+
+
 if __name__ == "__main__":
     _profile_case()

@@ -264,3 +264,23 @@ def test_db_add_remove_and_queries():
     assert fdb.remove_common("double_r") and not fdb.is_common("double_r")
     assert fdb.remove_variation("scaled_linear")
     assert fdb.hash() == h0  # back to the loaded definitions
+
+
+def test_denoiser_weight_file_reader(tmp_path):
+    """rfk_denoiser_read_params reads the committed weights and other .npz
+    layouts (stored or compressed, float16 or float32) exactly as numpy."""
+    from refraktor_gb300 import denoise as dn
+
+    path = Path(lr.__file__).resolve().parent / "workloads" / "denoiser_weights.npz"
+    np.testing.assert_array_equal(dn.read_params(path), np.load(path)["params"].astype(np.float32))
+    halves = np.array([0.0, -0.0, 1.0, -2.5, 6.1e-5, 5.96e-8, -3.0e-7, 65504.0, np.inf, -np.inf], dtype=np.float16)
+    np.savez(tmp_path / "stored.npz", params=halves)
+    np.testing.assert_array_equal(dn.read_params(tmp_path / "stored.npz"), halves.astype(np.float32))
+    full = np.random.default_rng(0).standard_normal(5000).astype(np.float32)
+    np.savez_compressed(tmp_path / "deflated.npz", params=full)
+    np.testing.assert_array_equal(dn.read_params(tmp_path / "deflated.npz"), full)
+    np.savez(tmp_path / "other.npz", weights=full)
+    with pytest.raises(_lib.RfkError):
+        dn.read_params(tmp_path / "other.npz")  # no params member
+    with pytest.raises(_lib.RfkError):
+        dn.read_params(tmp_path / "missing.npz")
