@@ -26,6 +26,15 @@ extern "C" {
 
 typedef struct rfk_denoiser rfk_denoiser;
 
+/* denoiser::make(name, dims, flags, stream) by registered name
+ * (interface/denoiser.h:21-39, factory.h:71-98). Registered:
+ * "rfkt::gb300_unet_denoiser", the U-Net below, with the weights of the .npz
+ * file `weights_path` (rfk_denoiser_read_params) or, when it is NULL, seeded
+ * initial weights. An unknown name returns RFK_E_INVALID with *out = NULL
+ * (the reference's factory returns a null pointer). */
+rfk_status rfk_denoiser_make(const char* name, const char* weights_path, rfk_denoiser** out);
+/* Registered name number `index` (0-based) into buf; RFK_E_INVALID past the end. */
+rfk_status rfk_denoiser_name(int index, char* buf, size_t cap);
 /* A network with seeded He-initialised weights. */
 rfk_status rfk_denoiser_create(uint64_t seed, rfk_denoiser** out);
 void rfk_denoiser_destroy(rfk_denoiser* d);

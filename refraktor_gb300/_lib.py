@@ -145,6 +145,8 @@ SIGNATURES = {
     "rfk_write_png": (C.c_int, [C.c_char_p, C.c_void_p, C.c_uint32, C.c_uint32, C.c_int]),
     # rfk_denoise.h
     "rfk_denoiser_create": (C.c_int, [C.c_uint64, C.POINTER(C.c_void_p)]),
+    "rfk_denoiser_make": (C.c_int, [C.c_char_p, C.c_char_p, C.POINTER(C.c_void_p)]),
+    "rfk_denoiser_name": (C.c_int, [C.c_int, C.c_char_p, C.c_size_t]),
     "rfk_denoiser_destroy": (None, [C.c_void_p]),
     "rfk_denoiser_param_count": (C.c_size_t, [C.c_void_p]),
     "rfk_denoiser_get_params": (C.c_int, [C.c_void_p, C.c_void_p, C.c_size_t]),

@@ -25,6 +25,7 @@
 
 #include <algorithm>
 #include <cmath>
+#include <cstdio>
 #include <cstring>
 #include <map>
 #include <memory>
@@ -290,6 +291,43 @@ void check_dims(uint32_t n, uint32_t w, uint32_t h, bool train) {
 }  // namespace
 
 extern "C" {
+
+namespace {
+const char* const kDenoiserNames[] = {"rfkt::gb300_unet_denoiser"};
+}  // namespace
+
+rfk_status rfk_denoiser_name(int index, char* buf, size_t cap) {
+    return guard([&] {
+        if (index < 0 || index >= (int)(sizeof kDenoiserNames / sizeof kDenoiserNames[0]))
+            fail(RFK_E_INVALID, "no denoiser with that index");
+        if (!buf || cap == 0) fail(RFK_E_INVALID, "null buffer");
+        std::snprintf(buf, cap, "%s", kDenoiserNames[index]);
+    });
+}
+
+rfk_status rfk_denoiser_make(const char* name, const char* weights_path, rfk_denoiser** out) {
+    if (out) *out = nullptr;
+    if (!name || !out) return guard([] { fail(RFK_E_INVALID, "null argument"); });
+    if (std::strcmp(name, kDenoiserNames[0]) != 0)
+        return guard([&] { fail(RFK_E_INVALID, std::string("unknown denoiser '") + name + "'"); });
+    std::vector<float> params;
+    if (weights_path) {
+        size_t n = 0;
+        if (rfk_status r = rfk_denoiser_read_params(weights_path, nullptr, 0, &n)) return r;
+        params.resize(n);
+        if (rfk_status r = rfk_denoiser_read_params(weights_path, params.data(), n, &n)) return r;
+    }
+    rfk_denoiser* d = nullptr;
+    if (rfk_status r = rfk_denoiser_create(0, &d)) return r;
+    if (weights_path) {
+        if (rfk_status r = rfk_denoiser_set_params(d, params.data(), params.size())) {
+            rfk_denoiser_destroy(d);
+            return r;
+        }
+    }
+    *out = d;
+    return RFK_OK;
+}
 
 rfk_status rfk_denoiser_create(uint64_t seed, rfk_denoiser** out) {
     return guard([&] {

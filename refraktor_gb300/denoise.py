@@ -43,6 +43,16 @@ class denoiser:
             lib().rfk_denoiser_destroy(self._h)
             self._h = None
 
+    @classmethod
+    def make(cls, name: str, weights_path: str | Path | None = None) -> "denoiser":
+        """denoiser::make by registered name (factory.h:71-98); raises
+        RfkError for an unknown name."""
+        h = C.c_void_p()
+        check(lib().rfk_denoiser_make(name.encode(), str(weights_path).encode() if weights_path else None, C.byref(h)))
+        d = cls.__new__(cls)
+        d._h = h
+        return d
+
     def param_count(self) -> int:
         return int(lib().rfk_denoiser_param_count(self._h))
 
@@ -265,6 +275,14 @@ def _profile_case(argv=None) -> None:
     e1.record()
     torch.cuda.synchronize()
     print(f"{a.case}: {e0.elapsed_time(e1) / a.reps:.3f} ms per call")
+
+
+def names() -> list[str]:
+    """The registered denoiser names."""
+    out, buf = [], C.create_string_buffer(256)
+    while lib().rfk_denoiser_name(len(out), buf, 256) == 0:
+        out.append(buf.value.decode())
+    return out
 
 
 def read_params(path: str | Path) -> np.ndarray:

@@ -284,3 +284,14 @@ def test_denoiser_weight_file_reader(tmp_path):
         dn.read_params(tmp_path / "other.npz")  # no params member
     with pytest.raises(_lib.RfkError):
         dn.read_params(tmp_path / "missing.npz")
+
+
+def test_denoiser_factory_names():
+    """denoiser::make by name (factory.h:71-98): the registry lists the U-Net,
+    and an unknown name fails before any device work."""
+    from refraktor_gb300 import denoise as dn
+
+    assert dn.names() == ["rfkt::gb300_unet_denoiser"]
+    with pytest.raises(_lib.RfkError) as e:
+        dn.denoiser.make("rfkt::oidn_denoiser")
+    assert e.value.code == 1 and "unknown denoiser" in str(e.value)

@@ -3,6 +3,7 @@ pass, loss and parameter gradients against the float64 CPU restatement of the
 same network (oracle/unet.py) with the GPU's bf16 storage points, training
 reducing the loss, and the denoise call's output."""
 import ctypes as C
+from pathlib import Path
 
 import numpy as np
 import pytest
@@ -11,6 +12,7 @@ torch = pytest.importorskip("torch")
 
 from oracle import unet as oref
 from refraktor_gb300 import _lib
+from refraktor_gb300 import denoise as dn
 
 pytestmark = pytest.mark.gpu
 
@@ -154,3 +156,12 @@ def test_trained_network_beats_the_plain_low_spp_image():
         net.denoise(bins[i], base[i], out, 32.0)
         gains.append(dn.psnr(out, tgt[i]) - dn.psnr(base[i], tgt[i]))
     assert np.mean(gains) > 2.0 and min(gains) > 0.0, gains
+
+
+def test_factory_makes_the_trained_network():
+    path = Path(dn.__file__).resolve().parent / "workloads" / "denoiser_weights.npz"
+    d = dn.denoiser.make("rfkt::gb300_unet_denoiser", path)
+    np.testing.assert_array_equal(d.params(), dn.read_params(path))
+    fresh = dn.denoiser.make("rfkt::gb300_unet_denoiser")
+    assert fresh.param_count() == d.param_count()
+
