@@ -28,7 +28,7 @@ PARAM_SLOTS = {n: 0 for n in ["linear", "sinusoidal", "spherical", "swirl", "hor
 
 def build() -> Path:
     so = HERE / "liboracle.so"
-    src = [HERE / "oracle.c", HERE / "oracle.h"]
+    src = [HERE / "oracle.c", HERE / "oracle.h", HERE / "Makefile"]
     if not so.exists() or any(p.stat().st_mtime > so.stat().st_mtime for p in src):
         subprocess.run(["make", "-C", str(HERE), "-s"], check=True)
     return so

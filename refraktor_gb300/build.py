@@ -69,11 +69,12 @@ def build(verbose: bool = False) -> Path:
     jobs: list[tuple[Path, list[str], list[Path]]] = []
     inc = [f"-I{CUDA / 'include'}", f"-I{PKG.parent / 'include'}"]
     cxx = os.environ.get("CXX", "g++")
-    cflags = ["-std=c++20", "-O2", "-fPIC", "-Wall", "-Wno-unused-function"] + inc
+    # no FMA contraction: host arithmetic gives the same bits on x86-64 and aarch64
+    cflags = ["-std=c++20", "-O2", "-ffp-contract=off", "-fPIC", "-Wall", "-Wno-unused-function"] + inc
     for src in HOST_SOURCES:
         s = CSRC / "host" / src
         o = BUILD / (src + ".o")
-        jobs.append((o, [cxx, *cflags, "-c", str(s), "-o", str(o)], [s, *headers]))
+        jobs.append((o, [cxx, *cflags, "-c", str(s), "-o", str(o)], [s, *headers, Path(__file__)]))
     o = BUILD / "jit_sources.o"
     jobs.append((o, [cxx, "-std=c++20", "-O1", "-fPIC", "-c", str(jit), "-o", str(o)], [jit]))
     nvcc = str(CUDA / "bin" / "nvcc")
