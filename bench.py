@@ -44,8 +44,9 @@ WORKLOAD = "plain 1080p single flame: 1920x1080, 1024 spp, 8 xforms + final xfor
 
 
 # dram__bytes_read.sum + dram__bytes_write.sum of one 1024-spp rfk_bin launch of
-# this workload (ncu, one pass; profiles/rfk_bin_1080p_launch_list.md)
-BIN_DRAM_BYTES_PER_LAUNCH = 39.30e6 + 40.45e3
+# this workload at the bench's launch shape (608 x 256, 8 chains per thread,
+# flush 1, block sort; ncu, one pass; profiles/rfk_bin_1080p_launch_list.md)
+BIN_DRAM_BYTES_PER_LAUNCH = 46.70e6 + 148.53e6
 # smsp__inst_executed.sum / chain steps of one 16-spp rfk_bin launch of this
 # workload at the bench's launch shape (608 x 256, 8 chains per thread, flush
 # 1, block sort): 451.1 M warp instructions for 36.77 M chain steps (ncu;
