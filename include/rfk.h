@@ -195,11 +195,15 @@ typedef struct {
 /* flame_kernel::bin(stream, state, bailout, temporal_slicing)
  *   flame_compiler.h:98, flame_compiler.cpp:866-955
  * rfk_bin enqueues and waits; rfk_bin_async enqueues, rfk_bin_wait waits for
- * the last enqueued call's result. Repeated calls keep accumulating. */
+ * its result. One call per state at a time: rfk_bin_async fails with
+ * RFK_E_INVALID while an earlier call on the state has not been waited for.
+ * Repeated calls keep accumulating. */
 rfk_status rfk_bin(rfk_state* s, const rfk_bailout* bo, void* stream, rfk_bin_result* out);
 rfk_status rfk_bin_async(rfk_state* s, const rfk_bailout* bo, void* stream);
 rfk_status rfk_bin_wait(rfk_state* s, rfk_bin_result* out);
-/* saved_state::abort_binning()  flame_compiler.h:85-88: safe from any thread. */
+/* saved_state::abort_binning()  flame_compiler.h:85-88: safe from any thread.
+ * Stops the call enqueued last, whenever it is issued after rfk_bin_async
+ * returns (also before the launch starts, while the stream is still busy). */
 rfk_status rfk_state_abort(rfk_state* s);
 /* Device pointer of the float4 histogram (w * h * 4 floats, row-major). */
 float* rfk_state_bins(rfk_state* s);
@@ -229,8 +233,9 @@ rfk_status rfk_prepare_samples(const rfk_kernel* k, const double* samples, size_
  * temporaries (FP64 samples, spline segments, schedule, output blocks) live
  * in a fixed 4 MiB array that every device using the library holds until
  * exit; requests that need more fail with RFK_E_INVALID and say how much they
- * need. The first call on a device takes the array's device address (make it
- * before any stream capture). Calls share the array and run on the legacy
+ * need. Every call looks up the array's device address on the current device;
+ * the first call on a device also loads the library's module there, so make
+ * it before any stream capture. Calls share the array and run on the legacy
  * default stream, blocking until the output is on the host: calls that could
  * overlap on the GPU (from several threads or processes) race on the array.
  * Every region is fully written before it is read, so nothing needs clearing. */

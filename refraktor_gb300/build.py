@@ -24,7 +24,7 @@ ARCH = "-gencode=arch=compute_103a,code=sm_103a"
 HOST_SOURCES = ["dsl.cpp", "value.cpp", "inflate.cpp", "flamedb.cpp", "genome.cpp", "align.cpp", "flam3.cpp", "codegen.cpp",
                 "runtime.cpp", "batch.cpp", "denoiser.cpp", "image_io.cpp",
                 "weights_io.cpp"]
-CUDA_SOURCES = {"image.cu": [], "tonemap_fast.cu": ["--use_fast_math"], "noalloc.cu": [], "unet_tc.cu": [],
+CUDA_SOURCES = {"image.cu": [], "tonemap_fast.cu": ["--use_fast_math"], "noalloc.cu": ["--fmad=false"], "unet_tc.cu": [],
                 "unet_ops.cu": []}
 JIT_TEXTS = {"rfk_src_device": "rfk_device.cuh", "rfk_src_iterate": "rfk_iterate.cuh"}
 

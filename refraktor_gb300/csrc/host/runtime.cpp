@@ -93,6 +93,26 @@ struct call_scope {
     }
 };
 
+// Stream-ordered temporaries of one call: allocated with cudaMallocAsync and
+// released with cudaFreeAsync on the same stream on every exit path, so a
+// check that throws between the allocations and the end of the call leaks
+// nothing (the frees are ordered after whatever the call already queued).
+struct stream_scope {
+    cudaStream_t s;
+    std::vector<void*> bufs;
+    explicit stream_scope(cudaStream_t st) : s(st) {}
+    template <class T>
+    T* alloc(size_t bytes, const char* what) {
+        void* p = nullptr;
+        cuda_check(cudaMallocAsync(&p, bytes, s), what);
+        bufs.push_back(p);
+        return static_cast<T*>(p);
+    }
+    ~stream_scope() {
+        for (void* p : bufs) cudaFreeAsync(p, s);
+    }
+};
+
 }  // namespace
 
 struct rfk_state {
@@ -314,14 +334,11 @@ void prepare(const kernel_impl& k, const double* samples, size_t nsamples, const
     const unsigned nseg = (unsigned)(nsamples - 3);
     for (unsigned sg : seg)
         if (sg >= nseg) fail(RFK_E_INVALID, "segment index out of range");
-    double* d_samples = nullptr;
-    float4* d_coeff = nullptr;
-    unsigned* d_seg = nullptr;
-    float* d_t = nullptr;
-    cuda_check(cudaMallocAsync(&d_samples, host.size() * sizeof(double), s), "alloc samples");
-    cuda_check(cudaMallocAsync(&d_coeff, (size_t)nseg * sample_size * sizeof(float4), s), "alloc coefficients");
-    cuda_check(cudaMallocAsync(&d_seg, seg.size() * sizeof(unsigned), s), "alloc schedule");
-    cuda_check(cudaMallocAsync(&d_t, t.size() * sizeof(float), s), "alloc schedule");
+    stream_scope tmp(s);
+    double* d_samples = tmp.alloc<double>(host.size() * sizeof(double), "alloc samples");
+    float4* d_coeff = tmp.alloc<float4>((size_t)nseg * sample_size * sizeof(float4), "alloc coefficients");
+    unsigned* d_seg = tmp.alloc<unsigned>(seg.size() * sizeof(unsigned), "alloc schedule");
+    float* d_t = tmp.alloc<float>(t.size() * sizeof(float), "alloc schedule");
     cuda_check(cudaMemcpyAsync(d_samples, host.data(), host.size() * sizeof(double), cudaMemcpyHostToDevice, s), "H2D samples");
     cuda_check(cudaMemcpyAsync(d_seg, seg.data(), seg.size() * sizeof(unsigned), cudaMemcpyHostToDevice, s), "H2D schedule");
     cuda_check(cudaMemcpyAsync(d_t, t.data(), t.size() * sizeof(float), cudaMemcpyHostToDevice, s), "H2D schedule");
@@ -331,10 +348,6 @@ void prepare(const kernel_impl& k, const double* samples, size_t nsamples, const
     launch(k.f_prepare, (unsigned)seg.size(), 256, s, args, "rfk_prepare");
     // the host vectors must outlive the copies
     cuda_check(cudaStreamSynchronize(s), "prepare");
-    cudaFreeAsync(d_samples, s);
-    cudaFreeAsync(d_coeff, s);
-    cudaFreeAsync(d_seg, s);
-    cudaFreeAsync(d_t, s);
 }
 
 void copy_out(char* buf, size_t cap, size_t* len, const std::string& s) {
@@ -644,11 +657,20 @@ rfk_status rfk_bin_async(rfk_state* st, const rfk_bailout* bo, void* stream) {
         if (!(bo->quality >= 0.0)) fail(RFK_E_INVALID, "quality must be >= 0");
         if (bo->quality == 0.0 && bo->iters == 0 && bo->millis == 0)
             fail(RFK_E_INVALID, "bailout needs a quality, pass or time limit");
+        // one call at a time per state: a second call would re-record the
+        // completion event and overwrite the pinned counters of the first
+        if (st->pending) fail(RFK_E_INVALID, "a bin call is pending on this state: call rfk_bin_wait first");
         const kernel_impl& k = *st->k;
         cudaStream_t s = (cudaStream_t)stream;
+        // The stop flag is cleared here, on the host, before anything is
+        // queued: an rfk_state_abort issued at any time after this call
+        // returns reaches the launch, even when earlier work keeps the
+        // stream busy (a clear queued on the stream could run after the
+        // abort and wipe it out). No launch of this state reads the flag now:
+        // the previous call has been waited for.
+        *reinterpret_cast<volatile unsigned*>(st->h_stop) = 0u;
         cuda_check(rfk_launch_clear_counters(st->d_counters, s), "clear counters");
         cuda_check(cudaMemsetAsync(st->d_counters + kCounterWords, 0, 98 * sizeof(unsigned long long), s), "clear histogram");
-        cuda_check(cudaMemsetAsync(st->d_stop, 0, sizeof(unsigned), s), "clear stop flag");
         dev_bin_args a{};
         a.samples = st->d_samples;
         a.st = {st->d_x, st->d_y, st->d_c, st->d_last};

@@ -11,21 +11,22 @@
 // The array is RFK_NOALLOC_SCRATCH_BYTES (4 MiB) on every device that loads
 // the library, held until the process exits. Host code must not use the
 // array's name as a device address: it is a host-side stand-in. The device
-// address is taken once per device with cudaGetSymbolAddress, with that
-// device current, on the first call that needs it.
+// address is asked for with cudaGetSymbolAddress on every call, with the
+// caller's device current: a cheap lookup once the module is loaded, and
+// never stale, also after cudaDeviceReset or any teardown of the primary
+// context reloads the module at another address. The first call on a device
+// loads the module there, so it should come before any stream capture.
+//
+// This file is built without FMA contraction (--fmad=false) so that
+// fix_rotation_kernel rounds every product and sum as the host fix_rotation
+// does (host code is built with -ffp-contract=off).
 #include <cuda_runtime.h>
-
-#include <mutex>
 
 #include "image_kernels.h"
 
 static __device__ __align__(256) unsigned char rfk_noalloc_scratch[RFK_NOALLOC_SCRATCH_BYTES];
 
 namespace {
-
-constexpr int kMaxDevices = 64;
-std::mutex g_scratch_mu;
-void* g_scratch_addr[kMaxDevices] = {};
 
 // FP64 rewrite of every affine's linear columns to (angle, log magnitude),
 // unwrapped across the samples, and of the palette hues across +-180 degrees:
@@ -72,18 +73,10 @@ __global__ void fix_rotation_kernel(double* __restrict__ s, unsigned n, unsigned
 }  // namespace
 
 extern "C" cudaError_t rfk_noalloc_scratch_address(void** addr, size_t* bytes) {
-    int dev = 0;
-    cudaError_t e = cudaGetDevice(&dev);
+    void* p = nullptr;
+    const cudaError_t e = cudaGetSymbolAddress(&p, rfk_noalloc_scratch);
     if (e != cudaSuccess) return e;
-    if (dev < 0 || dev >= kMaxDevices) return cudaErrorInvalidDevice;
-    std::lock_guard<std::mutex> lk(g_scratch_mu);
-    if (!g_scratch_addr[dev]) {
-        void* p = nullptr;
-        e = cudaGetSymbolAddress(&p, rfk_noalloc_scratch);
-        if (e != cudaSuccess) return e;
-        g_scratch_addr[dev] = p;
-    }
-    *addr = g_scratch_addr[dev];
+    *addr = p;
     *bytes = RFK_NOALLOC_SCRATCH_BYTES;
     return cudaSuccess;
 }

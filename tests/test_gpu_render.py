@@ -86,6 +86,47 @@ def test_abort_from_another_thread(db, comp):
     assert time.time() - t0 < 10
 
 
+def test_abort_right_after_bin_async_on_a_busy_stream(db, comp):
+    """An abort issued as soon as bin_async returns, while earlier work (a
+    500 ms time-budget bin of another state) still occupies the stream, stops
+    the new call at its first check: the stop flag is cleared on the host
+    before the call queues anything, so nothing queued later can wipe out the
+    abort."""
+    import torch
+
+    f = lr.flame.from_json(db, syn.plain_flame(2))
+    k = comp.get_flame_kernel(db, f)
+    s = torch.cuda.Stream()
+    busy = k.warmup(f.pack_samples(4, 64, 64), (64, 64), seed=5, count=10, stream=s)
+    st = k.warmup(f.pack_samples(4, 64, 64), (64, 64), seed=6, count=10, stream=s)
+    k.bin_async(busy, lr.bailout_args(iters=0, millis=500, quality=0), stream=s)
+    k.bin_async(st, lr.bailout_args(iters=0, millis=20000, quality=0), stream=s)
+    st.abort_binning()
+    t0 = time.time()
+    rb = busy.wait()
+    r = st.wait()
+    assert rb.status & 2
+    assert r.status & 4, r
+    assert r.elapsed_ms < 1000, r
+    assert time.time() - t0 < 5
+
+
+def test_second_bin_async_while_pending_is_rejected(db, comp):
+    """One bin call per state at a time: a second bin_async before the first
+    is waited for fails and leaves the pending call and its result intact."""
+    f = lr.flame.from_json(db, syn.plain_flame(2))
+    k = comp.get_flame_kernel(db, f)
+    st = k.warmup(f.pack_samples(4, 64, 64), (64, 64), seed=3, count=10)
+    k.bin_async(st, lr.bailout_args(iters=0, millis=0, quality=2.0))
+    with pytest.raises(lr.RfkError):
+        k.bin_async(st, lr.bailout_args(iters=0, millis=0, quality=2.0))
+    r = st.wait()
+    assert r.status & 1 and r.quality >= 2.0
+    assert abs(st.quality - r.quality) < 1e-9
+    r2 = k.bin(st, lr.bailout_args(iters=0, millis=0, quality=1.0))
+    assert r2.status & 1
+
+
 def test_deterministic_with_pass_cap(db, comp):
     g = syn.plain_flame(4)
     f = lr.flame.from_json(db, g)
