@@ -53,11 +53,33 @@ BIN_DRAM_BYTES_PER_LAUNCH = 46.70e6 + 148.53e6
 # the --ncu-case launch); each SM sub-partition issues one warp instruction per
 # clock
 BIN_WARP_INST_PER_ITER = 451.10e6 / 36.77e6
+# dram__bytes_read.sum + dram__bytes_write.sum of one rfk_bin_batch launch of
+# each batched workload (ncu, one pass over the bench's own batch launch);
+# None until captured
+BATCH_DRAM_BYTES_PER_RUN: dict = {"anim": None, "hetero": None}
 
 def _dist():
     ws = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
     return ws, rank
+
+
+def _free_port() -> int:
+    import socket
+
+    with socket.socket() as s:
+        s.bind(("127.0.0.1", 0))
+        return s.getsockname()[1]
+
+
+def launch_ranks(n: int, argv: list[str]) -> int:
+    """`bench.py --gpus N` started outside torchrun: runs this script again
+    under torch.distributed.run with N ranks on this node (one process per
+    GPU, rendezvous on 127.0.0.1) and returns its exit code. Under torchrun
+    (WORLD_SIZE set) the ranks already exist and nothing is launched."""
+    cmd = [sys.executable, "-m", "torch.distributed.run", "--nnodes=1", f"--nproc-per-node={n}", "--master-addr",
+           "127.0.0.1", "--master-port", str(_free_port()), str(Path(__file__).resolve()), *argv]
+    return subprocess.call(cmd)
 
 
 def _init_dist(ws: int, backend: str = "nccl") -> None:
@@ -285,9 +307,34 @@ def run_gpu(args) -> dict:
     }
     if rank == 0 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(genome, seconds=args.cpu_seconds)
+    if rank == 0 and args.denoise_flames > 0:
+        line["denoise"] = denoise_leg(db, args.denoise_flames)
     if ws > 1:
         torch.distributed.destroy_process_group()
     return line if rank == 0 else {}
+
+
+def denoise_leg(db, flames: int) -> dict:
+    """The second half of the metric: s/frame to 40 dB PSNR at 1920x1080,
+    denoised 32-spp path (render + U-Net) against the plain path, on `flames`
+    held-out seeded flames of the 1080p workload's distribution, with the
+    plain render as the fallback of every frame the denoised path leaves below
+    40 dB (refraktor_gb300/workloads/train_denoiser.py:
+    evaluate_with_fallback). Device time per frame; rank 0 only."""
+    from refraktor_gb300 import denoise as dn
+    from refraktor_gb300.workloads import train_denoiser as td
+
+    t0 = time.perf_counter()
+    net = dn.denoiser.load(ROOT / "refraktor_gb300" / "workloads" / "denoiser_weights.npz")
+    gs = td.dataset(db, flames, td.EVAL_SEED0, 1920, 1080)
+    ev = td.evaluate_with_fallback(db, net, gs, 1920, 1080)
+    ev.pop("per_flame")
+    ev["metric"] = "s/frame to 40 dB PSNR at 1080p (denoised low-spp vs plain, plain fallback)"
+    ev["unit"] = "s/frame"
+    ev["input_spp"] = td.LOW_SPP
+    ev["reference_spp"] = td.HIGH_SPP
+    ev["wall_s"] = time.perf_counter() - t0
+    return ev
 
 
 def cpu_baseline(genome: dict, seconds: float = 12.0, threads: int | None = None) -> dict:
@@ -351,6 +398,25 @@ def batch_workload(lr, db, name: str):
     big = max(range(len(fl)), key=lambda i: fl[i]["width"] * fl[i]["height"] * fl[i]["spp"])
     tune = (al[big], samples[big], (fl[big]["width"], fl[big]["height"]))
     return al[0], np.concatenate(samples), units, HETERO_WORKLOAD, tune
+
+
+def batch_working_set(units, grid: int, chains_per_block: int, passes_per_item: int) -> int:
+    """Histogram bytes the persistent batch launch keeps under atomic traffic
+    at once, averaged over its draws: the queue hands items out unit after
+    unit, so while unit u is drawn the `grid` resident blocks work on about
+    grid / N_u + 1 units, N_u = the items u needs at one draw per chain step
+    (quality * pixels / (chains per block * passes per item)); each of those
+    holds a histogram of about u's size (16 B per pixel)."""
+    per_item = float(chains_per_block * passes_per_item)
+    num = den = 0.0
+    for U in units:
+        px = U.width * U.height
+        draws = U.quality * px
+        n_u = max(draws / per_item, 1.0)
+        active = min(float(len(units)), grid / n_u + 1.0)
+        num += draws * active * px * 16
+        den += draws
+    return int(max(num / max(den, 1.0), 4 << 20))
 
 
 def run_batch(args) -> dict:
@@ -436,7 +502,8 @@ def run_batch(args) -> dict:
             e2e_times.append(time.perf_counter() - t0)
             e2e_passes += tot.total_passes
     e2e_t, (e2e_passes,) = merge_ranks(sum(e2e_times), [e2e_passes])
-    peak_ops = lr.probe_red_v4(8 << 20, 512)
+    ws_bytes = batch_working_set(units, k.info["grid"], k.info["block"] * k.info["chains_per_thread"], ppi)
+    peak_ops = lr.probe_red_v4(ws_bytes, 512)
     achieved_ops = draws / max(kern_ms / 1e3, 1e-9)
     if rank != 0:
         return {}
@@ -453,7 +520,12 @@ def run_batch(args) -> dict:
                 "s_per_unit": e2e_t / args.steps / len(units), "h2d_bytes_per_step": int(samples.nbytes),
                 "d2h_bytes_per_step": int(info["image_bytes"])},
         "roofline": {"bound": "l2_atomic", "achieved": achieved_ops * 16 / 1e9, "peak": peak_ops * 16 / 1e9, "unit": "GB/s",
-                     "frac": achieved_ops / peak_ops, "traffic": None, "achieved_ops": achieved_ops, "peak_ops": peak_ops},
+                     "frac": achieved_ops / peak_ops, "traffic": BATCH_DRAM_BYTES_PER_RUN.get(args.workload),
+                     "achieved_ops": achieved_ops, "peak_ops": peak_ops, "peak_buffer_bytes": ws_bytes,
+                     "note": "red.global.add.v4.f32 payload (16 B per draw); peak = measured random red.v4 rate "
+                             "into a buffer of the launch's histogram working set (peak_buffer_bytes: the units "
+                             "drawn at once, weighted by draws); traffic = DRAM bytes of one rfk_bin_batch launch "
+                             "(ncu)"},
         "gpu_launches": info["launches_per_run"] * args.steps,
         "clocks": clocks.summary(),
         "draws_per_s": draws / t_total,
@@ -461,14 +533,18 @@ def run_batch(args) -> dict:
 
 
 DENOISE_WORKLOAD = ("learned denoiser at 1920x1080: 32-spp render + U-Net (trained weights "
-                    "refraktor_gb300/workloads/denoiser_weights.npz) vs the plain path's spp to 40 dB PSNR against an "
-                    "independent 4096-spp render, seeded held-out flames")
+                    "refraktor_gb300/workloads/denoiser_weights.npz), plain render as the fallback below 40 dB, vs the "
+                    "plain path's time to 40 dB PSNR against an independent 4096-spp render, seeded held-out flames")
 
 
 def run_denoise(args) -> dict:
-    """s/frame to 40 dB PSNR at 1080p: the plain path renders progressively to
-    32..4096 spp and the spp where it crosses 40 dB is interpolated; the
-    denoised path renders 32 spp and runs the U-Net. Both timed on the device."""
+    """s/frame to 40 dB PSNR at 1080p on `--flames` held-out flames: the plain
+    path renders progressively until its PSNR against an independent 4096-spp
+    render crosses 40 dB (spp and time interpolated on log2 spp); the denoised
+    path renders 32 spp and runs the U-Net, and a frame left below 40 dB
+    continues the plain render to the plain path's 40 dB spp and pays that
+    time too. `value` is the denoised path's mean device time per frame with
+    that fallback; the plain path's is beside it."""
     import torch
 
     from refraktor_gb300 import build
@@ -483,28 +559,21 @@ def run_denoise(args) -> dict:
     torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
     build.build()
     db = lr.flamedb()
-    net = dn.denoiser.load(ROOT / "refraktor_gb300" / "workloads" / "denoiser_weights.npz")
-    gs = td.dataset(db, args.flames, td.EVAL_SEED0, 1920, 1080)
     with ClockSampler(int(os.environ.get("LOCAL_RANK", "0"))) as clocks:
-        ev = td.evaluate(db, net, gs, 1920, 1080)
-    den_s = ev["denoised_s_per_frame"]
-    plain_s = ev["plain_s_per_frame_to_40db_median"]
+        ev = denoise_leg(db, args.flames)
+    net = dn.denoiser.load(ROOT / "refraktor_gb300" / "workloads" / "denoiser_weights.npz")
+    gs = td.dataset(db, min(args.flames, 8), td.EVAL_SEED0, 1920, 1080)
     e2e_s, h2d, d2h = _denoise_e2e(db, net, gs, td, args)
+    den_s = ev["s_per_frame_to_40db_denoised"]
     return {
-        "metric": "s/frame to 40 dB PSNR at 1080p (denoised low-spp vs plain)", "value": den_s, "unit": "s/frame",
-        "n_gpus": 1, "steps": len(gs), "warmup": 0, "ms_per_step": 1e3 * den_s, "higher_is_better": False,
+        "metric": ev["metric"], "value": den_s, "unit": "s/frame",
+        "n_gpus": 1, "steps": ev["flames"], "warmup": 0, "ms_per_step": 1e3 * den_s, "higher_is_better": False,
         "scaling": "weak", "vs_baseline": None, "dtype": "bf16", "data": "synthetic (seeded held-out flames)",
-        "config": {"workload": DENOISE_WORKLOAD, "flames": len(gs)},
-        "plain_s_per_frame_to_40db_median": plain_s,
-        "plain_spp_to_40db_median": ev["plain_spp_to_40db_median"],
-        "denoised_psnr_db_mean": ev["psnr_denoised_32spp_mean"],
-        "plain_psnr_db_mean": ev["psnr_plain_mean"],
-        "denoised_reaches_40db": ev["denoised_reaches_40db"],
-        "speedup_where_both_reach_40db_median": ev.get("speedup_where_both_reach_40db_median"),
-        "denoise_ms": ev["denoise_ms"], "plain_ms_per_spp": ev["plain_ms_per_spp"],
+        "config": {"workload": DENOISE_WORKLOAD, "flames": ev["flames"]},
+        **{k: v for k, v in ev.items() if k not in ("metric", "unit")},
         "e2e": {"value": e2e_s, "unit": "s/frame", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                 "path": "host genome samples -> warm-up + bin to 32 spp -> tonemap -> U-Net -> half4 image on the "
-                        "host, wall clock per frame"},
+                        "host, wall clock per frame (no fallback)"},
         "clocks": clocks.summary(),
     }
 
@@ -609,7 +678,8 @@ def main():
     ap.add_argument("--block", type=int, default=256)
     ap.add_argument("--sort", type=int, default=2)
     ap.add_argument("--minb", type=int, default=0, help="blocks_per_sm of the --ncu-case kernel (0 = library default)")
-    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--gpus", type=int, default=1,
+                    help="GPUs (ranks) of this node; outside torchrun, N > 1 relaunches under torch.distributed.run")
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
@@ -618,8 +688,16 @@ def main():
     ap.add_argument("--workload", default="hd", choices=["hd", "anim", "hetero", "denoise"],
                     help="hd: the 1080p single-flame bench (default); anim / hetero: the batched workloads; "
                          "denoise: the learned denoiser's s/frame to 40 dB")
-    ap.add_argument("--flames", type=int, default=8, help="evaluation flames of --workload denoise")
+    ap.add_argument("--flames", type=int, default=200, help="evaluation flames of --workload denoise")
+    ap.add_argument("--denoise-flames", type=int, default=200,
+                    help="held-out 1080p flames of the denoise key of the default run (0 = leave it out)")
     args = ap.parse_args()
+    if args.gpus > 1 and "WORLD_SIZE" not in os.environ:
+        sys.exit(launch_ranks(args.gpus, sys.argv[1:]))
+    ws, _ = _dist()
+    if ws != args.gpus and "WORLD_SIZE" in os.environ:
+        print(f"bench.py: --gpus {args.gpus} under a launcher with WORLD_SIZE {ws}; the ranks present run",
+              file=sys.stderr)
     if args.ncu_case:
         run_ncu_case(args)
         return

@@ -105,7 +105,9 @@ typedef struct {
     int chains_per_thread; /* 0 = 4 when sorting, else 1 */
     int flush;             /* histogram update: 0 = red.global.add.v4.f32 per draw, 1 = warp-aggregated,
                               2 = warp-aggregated into a per-block shared-memory cache of hot pixels,
-                              3 = the shared-memory cache without warp aggregation */
+                              3 = the shared-memory cache without warp aggregation, 4 = shared-memory
+                              sums for the pixels the block's own draws show to be hot, one red per
+                              draw elsewhere */
     int blocks_per_sm;     /* 0 = registers capped so that 1280 / block bin blocks fit per SM, and as
                               many run as fit; n > 0 = registers capped so that n fit, and at most n
                               run per SM (launch bounds) */
@@ -169,6 +171,18 @@ rfk_status rfk_warmup_adopt(const rfk_kernel* k, const double* samples, size_t n
                             uint32_t h, uint32_t seed, uint32_t warmup_count, int temporal_multiplier, void* stream,
                             rfk_state** out);
 void rfk_state_destroy(rfk_state* s);
+/* flame_kernel::warmup into an existing state (no reference counterpart: the
+ * reference makes a new saved_state per warmup). For a renderer that draws
+ * frame after frame at one size: the state's kernel, size and temporal
+ * multiplier stay; its parameter blocks are prepared again from the new host
+ * samples, the chains start again from the Hammersley points and run
+ * warmup_count passes, the counters and the accumulated quality restart at
+ * 0, and the histogram is cleared when `clear` is non-zero (kept otherwise,
+ * also an adopted one). Nothing is allocated, so the per-frame cost is the
+ * sample upload, the preparation and the warm-up launch. Fails with
+ * RFK_E_INVALID while a bin call on the state is pending. */
+rfk_status rfk_state_rewarm(rfk_state* s, const double* samples, size_t nsamples, uint32_t seed, uint32_t warmup_count,
+                            int clear, void* stream);
 
 /* flame_kernel::bailout_args  flame_compiler.h:92-96 */
 typedef struct {

@@ -98,15 +98,24 @@ def compile_module(src: str, name: str, kernels: list[str], flags: list[str], ar
 # Flames whose reference chaos-game module is built: genome maker (seeded),
 # image size, threads per block and blocks per SM (the grid is blocks per SM
 # x the 152 SMs of a GB300, fixed at compile time through TOTAL_THREADS).
-def _ref_flames() -> dict:
+# The reference's only real-world genome, assets/flames_test/electricsheep.247.50049.flam3
+# (fisheye, bubble, julia, post affines, gamma 4), imported with the library's
+# flam3 reader (flame_types.cpp:131-239 restated) and rendered at its own size.
+SHEEP = "assets/flames_test/electricsheep.247.50049.flam3"
+
+
+def _ref_flames(ref_root: Path) -> dict:
     sys.path.insert(0, str(HERE.parent))
+    from refraktor_gb300 import librefrakt as lr
     from refraktor_gb300 import synthetic as syn
 
     bench = json.loads((HERE.parent / "refraktor_gb300" / "workloads" / "hd_1080p.json").read_text())
+    sheep = lr.flame.import_flam3(lr.flamedb(), (Path(ref_root) / SHEEP).read_text()).serialize()
     return {
         "c0": (syn.plain_flame(0), 512, 512, 128, 8),
         "hd": (syn.hd_flame(21), 320, 180, 128, 8),
         "bench": (bench, 1920, 1080, 128, 8),
+        "sheep": (sheep, 800, 592, 128, 8),
     }
 
 
@@ -132,7 +141,7 @@ def build_flames(ref_root: Path) -> None:
 
     rel = "assets/kernels/refactor.cu"
     inc = Path(ref_root) / "assets" / "kernels" / "include" / "refrakt"
-    for tag, (g, w, h, tpb, bpmp) in _ref_flames().items():
+    for tag, (g, w, h, tpb, bpmp) in _ref_flames(ref_root).items():
         R = orc.size_reals(g)
         header = ref_flame.flame_header(Path(ref_root), g, orc.affine_indices(g))
         grid = bpmp * REF_SMS

@@ -105,6 +105,7 @@ SIGNATURES = {
     "rfk_warmup_adopt": (C.c_int, [C.c_void_p, C.POINTER(C.c_double), C.c_size_t, C.c_void_p, C.c_uint32, C.c_uint32,
                                    C.c_uint32, C.c_uint32, C.c_int, C.c_void_p, C.POINTER(C.c_void_p)]),
     "rfk_state_destroy": (None, [C.c_void_p]),
+    "rfk_state_rewarm": (C.c_int, [C.c_void_p, C.c_void_p, C.c_size_t, C.c_uint32, C.c_uint32, C.c_int, C.c_void_p]),
     "rfk_bin": (C.c_int, [C.c_void_p, C.POINTER(Bailout), C.c_void_p, C.POINTER(BinResult)]),
     "rfk_bin_async": (C.c_int, [C.c_void_p, C.POINTER(Bailout), C.c_void_p]),
     "rfk_bin_wait": (C.c_int, [C.c_void_p, C.POINTER(BinResult)]),

@@ -173,8 +173,13 @@ struct rfk_denoiser {
                    "conv");
     }
 
-    // Forward pass of the whole network on ws.x; the result in ws.out.
-    void forward(workspace& s, cudaStream_t st) {
+    // Forward pass of the whole network on ws.x; the result in ws.out. For
+    // inference (`infer`) the last convolution of each decoder level and of
+    // the bottleneck writes its output straight into the next level's
+    // concatenation at twice the resolution (the upsampling fused into its
+    // epilogue); training keeps the low-resolution activations, which the
+    // backward pass reads, and upsamples them in a pass of its own.
+    void forward(workspace& s, cudaStream_t st, bool infer = false) {
         const int n = s.n, H = s.h, W = s.w;
         const int H2 = H / 2, W2 = W / 2, H3 = H / 4, W3 = W / 4, H4 = H / 8, W4 = W / 8;
         const int R = RFK_UNET_RELU;
@@ -188,14 +193,27 @@ struct rfk_denoiser {
         conv(E3B, s.a3, H3, W3, n, 128, 0, s.cat3, 384, 256, R, st);
         cuda_check(rfk_unet_avgpool(s.cat3, n, H3, W3, 384, 256, 128, s.p3, st), "pool");
         conv(B1, s.p3, H4, W4, n, 128, 0, s.b1, 256, 0, R, st);
-        conv(B2, s.b1, H4, W4, n, 256, 0, s.b2, 256, 0, R, st);
-        cuda_check(rfk_unet_upsample(s.b2, n, H4, W4, 256, s.cat3, 384, 0, st), "upsample");
+        const int U = R | RFK_UNET_UP2;
+        if (infer) {
+            conv(B2, s.b1, H4, W4, n, 256, 0, s.cat3, 384, 0, U, st);
+        } else {
+            conv(B2, s.b1, H4, W4, n, 256, 0, s.b2, 256, 0, R, st);
+            cuda_check(rfk_unet_upsample(s.b2, n, H4, W4, 256, s.cat3, 384, 0, st), "upsample");
+        }
         conv(D3A, s.cat3, H3, W3, n, 384, 0, s.e3, 128, 0, R, st);
-        conv(D3B, s.e3, H3, W3, n, 128, 0, s.d3, 128, 0, R, st);
-        cuda_check(rfk_unet_upsample(s.d3, n, H3, W3, 128, s.cat2, 192, 0, st), "upsample");
+        if (infer) {
+            conv(D3B, s.e3, H3, W3, n, 128, 0, s.cat2, 192, 0, U, st);
+        } else {
+            conv(D3B, s.e3, H3, W3, n, 128, 0, s.d3, 128, 0, R, st);
+            cuda_check(rfk_unet_upsample(s.d3, n, H3, W3, 128, s.cat2, 192, 0, st), "upsample");
+        }
         conv(D2A, s.cat2, H2, W2, n, 192, 0, s.e2, 64, 0, R, st);
-        conv(D2B, s.e2, H2, W2, n, 64, 0, s.d2, 64, 0, R, st);
-        cuda_check(rfk_unet_upsample(s.d2, n, H2, W2, 64, s.cat1, 96, 0, st), "upsample");
+        if (infer) {
+            conv(D2B, s.e2, H2, W2, n, 64, 0, s.cat1, 96, 0, U, st);
+        } else {
+            conv(D2B, s.e2, H2, W2, n, 64, 0, s.d2, 64, 0, R, st);
+            cuda_check(rfk_unet_upsample(s.d2, n, H2, W2, 64, s.cat1, 96, 0, st), "upsample");
+        }
         conv(D1A, s.cat1, H, W, n, 96, 0, s.e1, 32, 0, R, st);
         conv(D1B, s.e1, H, W, n, 32, 0, s.d1, 32, 0, R, st);
         conv(L_OUT, s.d1, H, W, n, 32, 0, s.out, 32, 0, RFK_UNET_F32OUT, st);
@@ -508,7 +526,7 @@ rfk_status rfk_denoise(rfk_denoiser* d, const float* bins, const float* base, ui
         cuda_check(rfk_unet_features(reinterpret_cast<const float4*>(bins), reinterpret_cast<const float4*>(base), P,
                                      (float)spp, s.x, st),
                    "features");
-        d->forward(s, st);
+        d->forward(s, st, true);
         cuda_check(rfk_unet_to_image(s.out, reinterpret_cast<const float4*>(base), reinterpret_cast<const float4*>(bins), P,
                                      out, format, st),
                    "to image");

@@ -224,7 +224,7 @@ void check_options(const rfk_compile_opts& o) {
     const int block = o.block > 0 ? o.block : 256;
     if (block % 32 != 0 || block > 1024) fail(RFK_E_INVALID, "block must be a multiple of 32 up to 1024");
     if (o.chains_per_thread > 8 || o.chains_per_thread < 0) fail(RFK_E_INVALID, "chains_per_thread must be in [0, 8]");
-    if (o.flush < 0 || o.flush > 3) fail(RFK_E_INVALID, "flush must be 0, 1, 2 or 3");
+    if (o.flush < 0 || o.flush > 4) fail(RFK_E_INVALID, "flush must be 0, 1, 2, 3 or 4");
     if (o.blocks_per_sm < 0 || o.blocks_per_sm > 32) fail(RFK_E_INVALID, "blocks_per_sm must be in [0, 32]");
     if (o.blocks_per_sm * block > 2048) fail(RFK_E_INVALID, "blocks_per_sm x block exceeds 2048 threads per SM");
 }
@@ -651,6 +651,32 @@ rfk_status rfk_warmup_adopt(const rfk_kernel* kh, const double* samples, size_t 
 
 void rfk_state_destroy(rfk_state* s) { delete s; }
 
+rfk_status rfk_state_rewarm(rfk_state* st, const double* samples, size_t nsamples, uint32_t seed, uint32_t warmup_count,
+                            int clear, void* stream) {
+    return guard([&] {
+        if (!st || !samples) fail(RFK_E_INVALID, "null argument");
+        if (st->pending) fail(RFK_E_INVALID, "a bin call is pending on this state: call rfk_bin_wait first");
+        const kernel_impl& k = *st->k;
+        cudaStream_t s = (cudaStream_t)stream;
+        const unsigned nsmp = (unsigned)st->grid * (unsigned)st->tmul;
+        std::vector<unsigned> seg;
+        std::vector<float> t;
+        temporal_schedule(nsmp, (unsigned)(nsamples - 3), seg, t);
+        prepare(k, samples, nsamples, seg, t, seed, st->d_samples, s);
+        cuda_check(cudaMemsetAsync(st->d_last, 255, st->nchains, s), "init chains");
+        if (clear) cuda_check(cudaMemsetAsync(st->d_bins, 0, (size_t)st->w * st->h * sizeof(float4), s), "clear histogram");
+        cuda_check(cudaMemsetAsync(st->d_counters, 0, (kCounterWords + 98) * sizeof(unsigned long long), s), "clear counters");
+        st->seed = seed;
+        st->quality = 0.0;
+        st->call_id = 0;
+        dev_chains ch{st->d_x, st->d_y, st->d_c, st->d_last};
+        unsigned ww = st->w, hh = st->h, sd = seed, salt = k.salt, wc = warmup_count;
+        void* args[] = {&st->d_samples, &ch, &ww, &hh, &sd, &salt, &wc};
+        launch(k.f_warmup, nsmp, (unsigned)k.block, s, args, "rfk_warmup");
+        cuda_check(cudaStreamSynchronize(s), "warmup");
+    });
+}
+
 rfk_status rfk_bin_async(rfk_state* st, const rfk_bailout* bo, void* stream) {
     return guard([&] {
         if (!st || !bo) fail(RFK_E_INVALID, "null argument");
@@ -1018,7 +1044,8 @@ rfk_status rfk_autotune(const rfk_db* db, const rfk_flame* f, const double* samp
             }
         }
         struct cand { int block, cpt, flush, sort, minb; };
-        const cand cands[] = {{128, 8, 1, 2, 8}, {256, 8, 1, 2, 4}, {256, 4, 1, 2, 4}, {256, 2, 1, 2, 6},
+        const cand cands[] = {{256, 8, 4, 2, 4}, {256, 4, 4, 2, 5}, {128, 8, 4, 2, 8}, {256, 4, 4, 1, 5},
+                              {128, 8, 1, 2, 8}, {256, 8, 1, 2, 4}, {256, 4, 1, 2, 4}, {256, 2, 1, 2, 6},
                               {128, 4, 1, 2, 12}, {256, 4, 2, 2, 5}, {256, 4, 0, 2, 5}, {256, 4, 1, 1, 5}};
         double best_rate = -1.0, worst_rate = 1e300;
         int n = 0;

@@ -11,7 +11,8 @@
 // thread), RFK_FLUSH (0 = one red.global.add.v4.f32 per draw, 1 = warp-
 // aggregated red for lanes that hit the same pixel, 2 = warp-aggregated into a
 // per-block shared-memory cache of hot pixels, 3 = the cache without warp
-// aggregation), RFK_SORT (1 = sort each
+// aggregation, 4 = shared-memory sums for the pixels that the block's own
+// draws show to be hot, one red per draw elsewhere), RFK_SORT (1 = sort each
 // warp's chains by picked xform every pass, so a warp runs one xform at a
 // time instead of a divergent switch).
 //
@@ -424,7 +425,7 @@ __device__ __forceinline__ void rfk_block_sort(float4* __restrict__ chains, cons
 }
 #endif
 
-#if RFK_FLUSH >= 2
+#if RFK_FLUSH == 2 || RFK_FLUSH == 3
 // Shared-memory cache of hot pixels (one per block): direct-mapped slots keyed
 // by pixel index, claimed with atomicCAS while empty and never evicted until
 // the next flush, so adds into a claimed slot never race with its flush.
@@ -479,12 +480,152 @@ __device__ __forceinline__ void rfk_cache_add(rfk_cache& cc, float4* __restrict_
 }
 #endif
 
+#if RFK_FLUSH == 4
+// Per-block table of hot pixels. Flames put a large share of their draws on
+// few pixels (the 1080p bench genome: 3.4% on one pixel, 21% on 64), and
+// red.global.add on one address serialises in its L2 slice, so those draws
+// are summed in shared memory and go out as one red.global.add.v4.f32 per hot
+// pixel and check interval; every other draw is one red.v4 after a single
+// 16-byte table load, with no warp-wide matching of pixels.
+//   discovery  in the first RFK_DISC_PASSES passes of every check interval,
+//              the draws of slot 0 of each thread are counted per pixel in a
+//              hash table (linear probing, at most RFK_DISC_PROBES places);
+//   rebuild    after those passes (all threads, between barriers): the old
+//              sums are flushed, and every pixel counted RFK_HOT_MIN times or
+//              more becomes hot (at most RFK_HOT_MAX, the first two free ways
+//              of its bucket), the counts are cleared;
+//   draw       a draw to a hot pixel adds to its sums (RFK_HOT_COPIES copies,
+//              picked by lane, so that lanes on one pixel rarely wait on the
+//              same shared-memory word), any other draw is one red.v4.
+// The sums are also flushed at the end of every check interval, so they
+// always go to the histogram of the unit whose draws they hold.
+#define RFK_HOT_MAX 64
+#define RFK_HOT_BUCKETS 128  // two ways each
+#define RFK_HOT_COPIES 4
+#define RFK_HOT_MIN 2u
+#define RFK_DISC_SLOTS 1024
+#define RFK_DISC_PROBES 4
+#define RFK_DISC_PASSES 2
+#define RFK_HOT_EMPTY 0xFFFFFFFFu
+struct rfk_hot {
+    uint4 bucket[RFK_HOT_BUCKETS];                       // (pixel, sum slot, pixel, sum slot)
+    float acc[4][RFK_HOT_MAX * RFK_HOT_COPIES];          // channel, slot * copies + copy
+    unsigned dtag[RFK_DISC_SLOTS];                       // discovery: pixel or empty
+    unsigned dcnt[RFK_DISC_SLOTS];                       // discovery: draws counted
+    unsigned nhot;
+};
+
+__device__ __forceinline__ unsigned rfk_hot_bucket(unsigned idx) {
+    return (idx * 2654435761u) >> (32 - 7);  // RFK_HOT_BUCKETS = 2^7
+}
+
+__device__ __forceinline__ unsigned rfk_disc_hash(unsigned idx) {
+    return (idx * 0x85EBCA77u) >> (32 - 10);  // RFK_DISC_SLOTS = 2^10
+}
+
+// All threads of the block: empty table, zero sums, empty discovery.
+__device__ __forceinline__ void rfk_hot_clear(rfk_hot& hs) {
+    for (unsigned i = threadIdx.x; i < RFK_HOT_BUCKETS; i += RFK_BLOCK)
+        hs.bucket[i] = make_uint4(RFK_HOT_EMPTY, 0u, RFK_HOT_EMPTY, 0u);
+    for (unsigned i = threadIdx.x; i < RFK_HOT_MAX * RFK_HOT_COPIES; i += RFK_BLOCK)
+        hs.acc[0][i] = hs.acc[1][i] = hs.acc[2][i] = hs.acc[3][i] = 0.0f;
+    for (unsigned i = threadIdx.x; i < RFK_DISC_SLOTS; i += RFK_BLOCK) {
+        hs.dtag[i] = RFK_HOT_EMPTY;
+        hs.dcnt[i] = 0u;
+    }
+    if (threadIdx.x == 0) hs.nhot = 0u;
+}
+
+// All threads of the block, between barriers: the sums of every hot pixel go
+// out as one red.v4 each and are zeroed; with `clear` the table is emptied
+// too (each thread empties only the ways it flushed).
+__device__ __forceinline__ void rfk_hot_flush(rfk_hot& hs, float4* __restrict__ bins, bool clear) {
+    for (unsigned b = threadIdx.x; b < RFK_HOT_BUCKETS * 2; b += RFK_BLOCK) {
+        unsigned* w = reinterpret_cast<unsigned*>(&hs.bucket[b >> 1]) + 2 * (b & 1u);
+        const unsigned idx = w[0], slot = w[1];
+        if (idx == RFK_HOT_EMPTY) continue;
+        if (clear) w[0] = RFK_HOT_EMPTY;
+        float s[4] = {0.0f, 0.0f, 0.0f, 0.0f};
+#pragma unroll
+        for (int ch = 0; ch < 4; ch++)
+#pragma unroll
+            for (int c = 0; c < RFK_HOT_COPIES; c++) {
+                float& a = hs.acc[ch][slot * RFK_HOT_COPIES + c];
+                s[ch] += a;
+                a = 0.0f;
+            }
+        if (s[3] != 0.0f || s[0] != 0.0f || s[1] != 0.0f || s[2] != 0.0f) rfk_red_v4(bins + idx, s[0], s[1], s[2], s[3]);
+    }
+}
+
+// All threads of the block, uniformly, after the discovery passes: flush the
+// sums, then make the table from the discovery counts and clear them. Ends
+// with a barrier; the caller's draws before it must all be done (the first
+// barrier below waits for them).
+__device__ __forceinline__ void rfk_hot_rebuild(rfk_hot& hs, float4* __restrict__ bins) {
+    __syncthreads();
+    rfk_hot_flush(hs, bins, true);
+    if (threadIdx.x == 0) hs.nhot = 0u;
+    __syncthreads();
+    for (unsigned i = threadIdx.x; i < RFK_DISC_SLOTS; i += RFK_BLOCK) {
+        const unsigned idx = hs.dtag[i], n = hs.dcnt[i];
+        hs.dtag[i] = RFK_HOT_EMPTY;
+        hs.dcnt[i] = 0u;
+        if (idx == RFK_HOT_EMPTY || n < RFK_HOT_MIN) continue;
+        unsigned* w = reinterpret_cast<unsigned*>(&hs.bucket[rfk_hot_bucket(idx)]);
+        // claim a way first, then a sum slot: a pixel without a free way stays cold
+        int way = -1;
+        if (atomicCAS(&w[0], RFK_HOT_EMPTY, RFK_HOT_EMPTY - 1u) == RFK_HOT_EMPTY) way = 0;
+        else if (atomicCAS(&w[2], RFK_HOT_EMPTY, RFK_HOT_EMPTY - 1u) == RFK_HOT_EMPTY) way = 2;
+        if (way < 0) continue;
+        const unsigned slot = atomicAdd(&hs.nhot, 1u);
+        if (slot < RFK_HOT_MAX) {
+            w[way + 1] = slot;
+            w[way] = idx;
+        } else {
+            w[way] = RFK_HOT_EMPTY;  // table full: the claimed way stays free
+        }
+    }
+    __syncthreads();
+}
+
+// Counts one draw of a discovery pass.
+__device__ __forceinline__ void rfk_disc_count(rfk_hot& hs, unsigned idx) {
+    unsigned h = rfk_disc_hash(idx);
+#pragma unroll 1
+    for (int p = 0; p < RFK_DISC_PROBES; p++, h = (h + 1u) & (RFK_DISC_SLOTS - 1u)) {
+        unsigned t = hs.dtag[h];
+        if (t == RFK_HOT_EMPTY) t = atomicCAS(&hs.dtag[h], RFK_HOT_EMPTY, idx);
+        if (t == RFK_HOT_EMPTY || t == idx) {
+            atomicAdd(&hs.dcnt[h], 1u);
+            return;
+        }
+    }
+}
+#endif
+
 __device__ __forceinline__ void rfk_flush(float4* __restrict__ bins, int idx, float4 v
-#if RFK_FLUSH >= 2
+#if RFK_FLUSH == 2 || RFK_FLUSH == 3
                                           , rfk_cache& cc
+#elif RFK_FLUSH == 4
+                                          , rfk_hot& hs, bool disc
 #endif
 ) {
-#if RFK_FLUSH == 3
+#if RFK_FLUSH == 4
+    if (idx < 0) return;
+    const uint4 e = hs.bucket[rfk_hot_bucket((unsigned)idx)];
+    const unsigned slot = (e.x == (unsigned)idx) ? e.y : (e.z == (unsigned)idx) ? e.w : RFK_HOT_EMPTY;
+    if (slot != RFK_HOT_EMPTY) {
+        const unsigned a = slot * RFK_HOT_COPIES + (threadIdx.x & (RFK_HOT_COPIES - 1));
+        atomicAdd(&hs.acc[0][a], v.x);
+        atomicAdd(&hs.acc[1][a], v.y);
+        atomicAdd(&hs.acc[2][a], v.z);
+        atomicAdd(&hs.acc[3][a], v.w);
+    } else {
+        rfk_red_v4(bins + idx, v.x, v.y, v.z, v.w);
+    }
+    if (disc) rfk_disc_count(hs, (unsigned)idx);
+#elif RFK_FLUSH == 3
     if (idx >= 0) rfk_cache_add(cc, bins, idx, v);
 #elif RFK_FLUSH >= 1
     // lanes that hit the same pixel add their contributions first
@@ -560,8 +701,10 @@ struct rfk_pass_smem {
 #elif RFK_SORT == 2
     unsigned counts[2][RFK_NX * (RFK_BLOCK / 32)];  // ping-pong sets, one per pass parity
 #endif
-#if RFK_FLUSH >= 2
+#if RFK_FLUSH == 2 || RFK_FLUSH == 3
     rfk_cache cache;
+#elif RFK_FLUSH == 4
+    rfk_hot hot;
 #endif
     unsigned dummy;
 };
@@ -579,8 +722,10 @@ __device__ __forceinline__ void rfk_pass_smem_init(rfk_pass_smem& sm) {
 #if RFK_SORT == 2
     for (unsigned i = threadIdx.x; i < 2 * RFK_NX * (RFK_BLOCK / 32); i += RFK_BLOCK) (&sm.counts[0][0])[i] = 0u;
 #endif
-#if RFK_FLUSH >= 2
+#if RFK_FLUSH == 2 || RFK_FLUSH == 3
     rfk_cache_clear(sm.cache);
+#elif RFK_FLUSH == 4
+    rfk_hot_clear(sm.hot);
 #endif
 }
 
@@ -615,10 +760,24 @@ __device__ __forceinline__ void rfk_store_chains(const rfk_pass_smem& sm, const 
     }
 }
 
-#if RFK_FLUSH >= 2
+#if RFK_FLUSH == 2 || RFK_FLUSH == 3
 #define RFK_CACHE_ARG , sm.cache
+#elif RFK_FLUSH == 4
+#define RFK_CACHE_ARG , sm.hot, disc
 #else
 #define RFK_CACHE_ARG
+#endif
+
+// Flush 4: the discovery passes of a check interval sample the draws of slot
+// 0; after the last of them the block rebuilds its hot-pixel table. Both
+// depend only on the pass number within the interval (block-uniform).
+#if RFK_FLUSH == 4
+#define RFK_DISC(it, q) ((it) < RFK_DISC_PASSES && (q) == 0)
+#define RFK_HOT_PASS_END(it, bins) \
+    if ((it) + 1 == RFK_DISC_PASSES) rfk_hot_rebuild(sm.hot, (bins));
+#else
+#define RFK_DISC(it, q) false
+#define RFK_HOT_PASS_END(it, bins)
 #endif
 
 // One pass over this thread's RFK_CPT chains, in two parts with the loop over
@@ -661,8 +820,9 @@ __device__ __forceinline__ void rfk_pick_sort(rfk_pass_smem& sm, const float* P,
 
 __device__ __forceinline__ void rfk_move_slot(int q, unsigned chain, rfk_pass_smem& sm, const float* P, float4* bins,
                                               unsigned w, unsigned h, unsigned call_id, unsigned long long pass,
-                                              unsigned seed, unsigned salt, bool draw, unsigned& my_hits,
+                                              unsigned seed, unsigned salt, bool draw, bool disc, unsigned& my_hits,
                                               unsigned& my_draws) {
+    (void)disc;
     float4* slot = &sm.chains[rfk_slot(q)];
     const float4 s = *slot;
     float x = s.x, y = s.y, c = s.z;
@@ -701,8 +861,10 @@ __device__ __forceinline__ void rfk_block_totals(unsigned& my_hits, unsigned& my
         atomicAdd(s_draws, (unsigned long long)wd);
     }
     __syncthreads();
-#if RFK_FLUSH >= 2
+#if RFK_FLUSH == 2 || RFK_FLUSH == 3
     rfk_cache_flush(sm.cache, bins);
+#elif RFK_FLUSH == 4
+    rfk_hot_flush(sm.hot, bins, false);
 #else
     (void)sm;
     (void)bins;
@@ -747,8 +909,9 @@ extern "C" __global__ void RFK_BIN_BOUNDS rfk_bin(rfk_bin_args a) {
 #pragma unroll 1
             for (int q = 0; q < RFK_CPT; q++)
                 rfk_move_slot(q, chain0 + (unsigned)q * cstride, sm, P, a.bins, a.w, a.h, a.call_id, pass, a.seed,
-                              a.salt, true, my_hits, my_draws);
+                              a.salt, true, RFK_DISC(it, q), my_hits, my_draws);
             pass++;
+            RFK_HOT_PASS_END(it, a.bins)
         }
         // bailout check: block totals -> global counters -> decision
         rfk_block_totals(my_hits, my_draws, &s_hits, &s_draws, sm, a.bins);
@@ -818,7 +981,7 @@ extern "C" __global__ void RFK_BIN_BOUNDS rfk_warmup(const float* __restrict__ s
 #pragma unroll 1
         for (int q = 0; q < RFK_CPT; q++) {
             rfk_move_slot(q, chain0 + (unsigned)q * cstride, sm, P, nullptr, w, h, 0xFFFEu, pass, seed, salt, false,
-                          no_hits, no_draws);
+                          false, no_hits, no_draws);
             // without the histogram updates (asm with a memory clobber) the
             // compiler would keep the flame parameters in registers across
             // passes: twice the registers, half the occupancy
@@ -880,9 +1043,10 @@ extern "C" __global__ void RFK_BIN_BOUNDS rfk_bin_tm(rfk_bin_args a) {
 #pragma unroll 1
             for (int q = 0; q < RFK_CPT; q++)
                 rfk_move_slot(q, chain0 + (unsigned)q * cstride, sm, P, a.bins, a.w, a.h, a.call_id, pass, a.seed,
-                              a.salt, true, my_hits, my_draws);
+                              a.salt, true, RFK_DISC(n, q), my_hits, my_draws);
             pass++;
             total++;
+            RFK_HOT_PASS_END(n, a.bins)
         }
         in_slice += n;
         rfk_block_totals(my_hits, my_draws, &s_hits, &s_draws, sm, a.bins);
@@ -1082,8 +1246,9 @@ extern "C" __global__ void RFK_BIN_BOUNDS rfk_bin_batch(rfk_batch_args a) {
 #pragma unroll 1
                 for (int q = 0; q < RFK_CPT; q++)
                     rfk_move_slot(q, chain0 + (unsigned)q * cstride, sm, P, U.bins, U.w, U.h, call_id, pass, a.seed,
-                                  a.salt, draw, my_hits, my_draws);
+                                  a.salt, draw, RFK_DISC(it, q), my_hits, my_draws);
                 pass++;
+                RFK_HOT_PASS_END(it, U.bins)
             }
             done += n;
             rfk_block_totals(my_hits, my_draws, &s_hits, &s_draws, sm, U.bins);

@@ -10,6 +10,8 @@
 
 #define RFK_UNET_RELU 1    // conv epilogue: ReLU after the bias
 #define RFK_UNET_F32OUT 2  // conv epilogue: store f32 instead of bf16
+#define RFK_UNET_UP2 4     // conv epilogue: store each output pixel at its 2x2 pixels of a (2h, 2w) output
+                           // (nearest upsampling into the next level's concatenation; bf16, no accumulate)
 
 #ifdef __cplusplus
 extern "C" {

@@ -50,6 +50,7 @@ struct conv_args {
     const float* bias;
     int relu;
     int out_f32;  // store f32 instead of bf16
+    int up2;      // store at the 2x2 pixels of a (2h, 2w) output
     const bf16* mask;
     int mask_cstride, mask_coff;
     int accumulate;
@@ -330,6 +331,14 @@ __global__ void __launch_bounds__(320, 1) conv3x3_tc(const __grid_constant__ CUt
                         for (int q = 0; q < 4; q++) {
                             float4 o = p.accumulate ? dst[q] : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
                             dst[q] = make_float4(v[4 * q] + o.x, v[4 * q + 1] + o.y, v[4 * q + 2] + o.z, v[4 * q + 3] + o.w);
+                        }
+                    } else if (p.up2) {
+                        // nearest 2x upsampling: the four pixels (2x + dx, 2y + dy) of the
+                        // output image, which is (2h, 2w)
+#pragma unroll
+                        for (int d = 0; d < 4; d++) {
+                            const size_t pix2 = ((size_t)img * 2 * p.h + 2 * y + (d >> 1)) * (2 * (size_t)p.w) + 2 * x + (d & 1);
+                            store_bf16x16(static_cast<bf16*>(p.out) + pix2 * p.out_cstride + p.out_coff + ch, v);
                         }
                     } else {
                         bf16* dst = static_cast<bf16*>(p.out) + at;
@@ -650,6 +659,8 @@ extern "C" cudaError_t rfk_unet_conv3x3(const void* in, int n_img, int h, int w,
     p.bias = bias;
     p.relu = flags & RFK_UNET_RELU;
     p.out_f32 = (flags & RFK_UNET_F32OUT) ? 1 : 0;
+    p.up2 = (flags & RFK_UNET_UP2) ? 1 : 0;
+    if (p.up2 && (p.out_f32 || accumulate)) return cudaErrorInvalidValue;
     p.mask = static_cast<const bf16*>(mask);
     p.mask_cstride = mask_cstride;
     p.mask_coff = mask_coff;

@@ -304,6 +304,15 @@ class saved_state:
     def abort_binning(self) -> None:
         check(lib().rfk_state_abort(self._h))
 
+    def rewarm(self, samples: np.ndarray, seed: int, count: int, clear: bool = True, stream=None) -> None:
+        """warmup into this state's buffers (rfk_state_rewarm): new samples,
+        same kernel and size, fresh chains and counters, histogram cleared
+        unless `clear` is False; allocates nothing."""
+        s = np.ascontiguousarray(samples, dtype=np.float64)
+        ss = self.kernel.info["size_reals"] + 768
+        check(lib().rfk_state_rewarm(self._h, s.ctypes.data, s.size // ss, seed & 0xFFFFFFFF, count, 1 if clear else 0,
+                                     _stream_ptr(stream)))
+
     def bins_ptr(self) -> int:
         return lib().rfk_state_bins(self._h)
 

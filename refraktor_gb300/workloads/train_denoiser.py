@@ -133,6 +133,110 @@ def evaluate(db, net, genomes, w: int, h: int, seed: int = 7) -> dict:
     return out
 
 
+FALLBACK_CHECKPOINTS = [32, 48, 64, 96, 128, 192, 256, 384, 512, 768, 1024, 1536, 2048, 3072, 4096]
+
+
+def evaluate_with_fallback(db, net, genomes, w: int, h: int, seed: int = 7, kernel=None) -> dict:
+    """Seconds per frame to 40 dB PSNR, denoised path against plain path, with
+    the plain path as the denoised path's fallback. Per flame (device time
+    with CUDA events on the render stream):
+      plain     warm-up + bin to the spp where the PSNR against an independent
+                4096-spp render first reaches 40 dB (interpolated on log2 spp
+                between checkpoints, the bin time likewise) + one tonemap;
+      denoised  warm-up + bin to 32 spp + tonemap + U-Net; a frame whose
+                denoised PSNR stays below 40 dB then continues the plain render
+                from its 32 spp to the plain path's 40 dB spp and tonemaps
+                again, and pays that time too.
+    Flames whose plain render stays below 40 dB at 4096 spp have no plain time
+    and are left out of both means (counted in `plain_never_reaches`)."""
+    import torch
+
+    from refraktor_gb300 import denoise as dn
+    from refraktor_gb300 import librefrakt as lr
+
+    fs = [lr.flame.from_json(db, g) for g in genomes]
+    if kernel is None:
+        opts, _ = lr.autotune(db, fs[0], fs[0].pack_samples(4, w, h), (w, h))
+        kernel = lr.flame_compiler().get_flame_kernel(db, fs[0], **opts)
+    k = kernel
+    tm = lr.tonemapper()
+    stream = torch.cuda.Stream()
+    img = torch.empty((h, w, 4), dtype=torch.float32, device="cuda")
+    ref = torch.empty((h, w, 4), dtype=torch.float32, device="cuda")
+    den = torch.empty((h, w, 4), dtype=torch.float32, device="cuda")
+
+    def timed(fn):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        out = fn()
+        e1.record(stream)
+        e1.synchronize()
+        return out, e0.elapsed_time(e1) / 1e3
+
+    rows = []
+    for i, f in enumerate(fs):
+        tp = f.tonemap_params()
+        tmargs = (tp["gamma"], tp["brightness"], tp["vibrancy"])
+        samples = f.pack_samples(4, w, h)
+        st_ref = k.warmup(samples, (w, h), seed=seed + 2 * i + 1, count=20, stream=stream)
+        k.bin(st_ref, lr.bailout_args(iters=0, millis=0, quality=HIGH_SPP), stream=stream)
+        tm.run(st_ref.bins(), ref, (w, h), st_ref.quality, *tmargs, fmt=lr.FLOAT4, stream=stream)
+        stream.synchronize()
+        del st_ref
+        st, t_warm = timed(lambda: k.warmup(samples, (w, h), seed=seed + 2 * i, count=20, stream=stream))
+        _, t_tm = timed(lambda: tm.run(st.bins(), img, (w, h), 1.0, *tmargs, fmt=lr.FLOAT4, stream=stream))
+        spp, t_bin, psnrs, den_db, t_den = [0.0], [0.0], [], None, None
+        for c in FALLBACK_CHECKPOINTS:
+            _, dt = timed(lambda: k.bin(st, lr.bailout_args(iters=0, millis=0, quality=c - st.quality), stream=stream))
+            spp.append(st.quality)
+            t_bin.append(t_bin[-1] + dt)
+            tm.run(st.bins(), img, (w, h), st.quality, *tmargs, fmt=lr.FLOAT4, stream=stream)
+            stream.synchronize()
+            psnrs.append(dn.psnr(img, ref))
+            if c == FALLBACK_CHECKPOINTS[0]:
+                _, t_den = timed(lambda: net.denoise(st.bins(), img, den, st.quality, stream=stream))
+                den_db = dn.psnr(den, ref)
+            if psnrs[-1] >= 40.0:
+                break
+        row = {"psnr_denoised": den_db, "psnr_plain": psnrs, "spp": spp[1:], "t_warmup": t_warm, "t_tonemap": t_tm,
+               "t_unet": t_den, "t_bin_32": t_bin[1]}
+        if psnrs[-1] >= 40.0:
+            j = len(psnrs) - 1
+            if j == 0:
+                s40, tb40 = spp[1], t_bin[1]
+            else:
+                a, b = psnrs[j - 1], psnrs[j]
+                fr = (40.0 - a) / (b - a) if b > a else 1.0
+                s40 = float(2 ** (np.log2(spp[j]) + fr * (np.log2(spp[j + 1]) - np.log2(spp[j]))))
+                tb40 = t_bin[j] + fr * (t_bin[j + 1] - t_bin[j])
+            plain = t_warm + tb40 + t_tm
+            dpath = t_warm + t_bin[1] + t_tm + t_den
+            if den_db < 40.0:
+                dpath += max(tb40 - t_bin[1], 0.0) + t_tm
+            row.update(spp_to_40db=s40, plain_s=plain, denoised_s=dpath)
+        rows.append(row)
+        del st
+    ok = [r for r in rows if "plain_s" in r]
+    plain = np.array([r["plain_s"] for r in ok])
+    dpath = np.array([r["denoised_s"] for r in ok])
+    pden = np.array([r["psnr_denoised"] for r in rows])
+    out = {
+        "flames": len(rows), "width": w, "height": h, "plain_never_reaches": len(rows) - len(ok),
+        "s_per_frame_to_40db_plain": float(plain.mean()) if ok else None,
+        "s_per_frame_to_40db_denoised": float(dpath.mean()) if ok else None,
+        "speedup": float(plain.mean() / dpath.mean()) if ok else None,
+        "speedup_per_flame_median": float(np.median(plain / dpath)) if ok else None,
+        "denoised_reaches_40db": float((pden >= 40.0).mean()),
+        "denoised_psnr_db_mean": float(pden.mean()), "denoised_psnr_db_median": float(np.median(pden)),
+        "plain_psnr_db_32spp_mean": float(np.mean([r["psnr_plain"][0] for r in rows])),
+        "plain_spp_to_40db_median": float(np.median([r["spp_to_40db"] for r in ok])) if ok else None,
+        "unet_ms_median": 1e3 * float(np.median([r["t_unet"] for r in rows])),
+        "render_32spp_ms_median": 1e3 * float(np.median([r["t_bin_32"] + r["t_warmup"] + r["t_tonemap"] for r in rows])),
+        "per_flame": rows,
+    }
+    return out
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--train", type=int, default=2000)

@@ -64,3 +64,23 @@ def test_merge_ranks_is_identity_for_one_process():
     import bench
 
     assert bench.merge_ranks(3.0, [5, 6], device="cpu") == (3.0, [5, 6])
+
+
+def test_gpus_flag_launches_its_own_ranks():
+    """bench.py --gpus 2 outside torchrun relaunches itself under
+    torch.distributed.run with two ranks (WORLD_SIZE 2): the reference arm
+    runs on rank 0, which prints the one JSON line, and rank 1 exits 0."""
+    import json
+    import subprocess
+
+    env = {k: v for k, v in os.environ.items() if k not in ("WORLD_SIZE", "RANK", "LOCAL_RANK", "MASTER_ADDR",
+                                                             "MASTER_PORT")}
+    r = subprocess.run([sys.executable, str(ROOT / "bench.py"), "--gpus", "2", "--impl", "reference", "--steps", "1",
+                        "--warmup", "0", "--cpu-seconds", "0.5"], capture_output=True, text=True, timeout=600, env=env,
+                       cwd=str(ROOT))
+    assert r.returncode == 0, r.stdout[-2000:] + r.stderr[-2000:]
+    lines = [json.loads(x) for x in r.stdout.splitlines() if x.startswith("{")]
+    assert len(lines) == 1, r.stdout
+    line = lines[0]
+    assert line["impl"] == "reference" and line["n_gpus"] == 2
+    assert line["config"]["parallelism"] == "rank 0 of 2"

@@ -101,7 +101,10 @@ def librfk_render(tag: str, seed: int, spp: float) -> np.ndarray:
     g, w, h = m["genome"], m["width"], m["height"]
     db = lr.flamedb()
     f = lr.flame.from_json(db, g)
-    k = lr.flame_compiler().get_flame_kernel(db, f, flush=1)
+    # the bench genome renders with the launch shape the bench uses (the
+    # autotuner's pick for it); the small flames with warp aggregation
+    opts = lr.autotune(db, f, f.pack_samples(4, w, h), (w, h))[0] if tag == "bench" else dict(flush=1)
+    k = lr.flame_compiler().get_flame_kernel(db, f, **opts)
     st = k.warmup(f.pack_samples(4, w, h), (w, h), seed=seed, count=WARMUP)
     r = k.bin(st, lr.bailout_args(iters=0, millis=0, quality=spp))
     assert r.status & 1, r
@@ -112,7 +115,12 @@ def _l1(a, b, c):
     return float(np.abs(a[..., c] / a[..., c].sum() - b[..., c] / b[..., c].sum()).sum())
 
 
-CASES = [("c0", 32.0, (3,)), ("hd", 256.0, (0, 1, 2, 3))]
+# config 0 (512x512), a config-1 flame at 320x180, the 1080p bench genome at
+# 1920x1080 (the configuration bench.py times), and the reference's own
+# real-world genome (assets/flames_test/electricsheep.247.50049.flam3 at its
+# size, 800x592: fisheye, bubble, julia, post affines)
+CASES = [("c0", 32.0, (3,)), ("hd", 256.0, (0, 1, 2, 3)), ("bench", 32.0, (0, 1, 2, 3)),
+         ("sheep", 64.0, (0, 1, 2, 3))]
 
 
 @pytest.mark.parametrize("tag,spp,channels", CASES)

@@ -93,6 +93,33 @@ def test_conv3x3_slices_mask_and_accumulate():
     assert torch.equal(out[..., :64], before[..., :64]) and torch.equal(out[..., 96:], before[..., 96:])
 
 
+@pytest.mark.parametrize("cin,cout", [(256, 256), (128, 128), (64, 64)])
+def test_conv3x3_fused_upsample_store(cin, cout):
+    """RFK_UNET_UP2: the epilogue stores each output pixel at its 2x2 pixels
+    of a (2h, 2w) output, in a channel slice of a wider tensor (the decoder's
+    concatenation): the same values as the convolution followed by nearest
+    upsampling, and the other channels untouched."""
+    L = _L()
+    g = torch.Generator(device="cuda").manual_seed(cin + 3)
+    n, h, w = 2, 6, 68
+    x = torch.randn(n, h, w, cin, device="cuda", generator=g).to(torch.bfloat16)
+    wt = (torch.randn(cout, 9, cin, device="cuda", generator=g) / np.sqrt(9 * cin)).to(torch.bfloat16)
+    b = torch.randn(cout, device="cuda", generator=g)
+    wide = cout + cout // 2
+    out = torch.randn(n, 2 * h, 2 * w, wide, device="cuda", generator=g).to(torch.bfloat16)
+    before = out.clone()
+    _conv(L, x, 0, cin, wt, cout, bias=b, relu=1 | 4, out=out, out_coff=0)
+    ref = torch.relu(_ref_conv(x, wt, b))
+    ref_up = ref.repeat_interleave(2, dim=1).repeat_interleave(2, dim=2)
+    _bf16_close(out[..., :cout], ref_up, float(ref.abs().max()))
+    assert torch.equal(out[..., cout:], before[..., cout:])
+    # f32 or accumulating outputs are not combined with the upsampling store
+    err = torch.zeros(1, dtype=torch.int32, device="cuda")
+    rc = L.rfk_unet_conv3x3(x.data_ptr(), n, h, w, cin, 0, cin, wt.data_ptr(), cout, b.data_ptr(), 1 | 2 | 4,
+                            out.data_ptr(), wide, 0, None, 0, 0, 0, err.data_ptr(), None)
+    assert rc != 0
+
+
 def test_conv3x3_input_gradient_with_flipped_weights():
     """dX of y = conv(x, W) is conv(dY, W'), W'[c][8 - t][n] = W[n][t][c]."""
     L = _L()
