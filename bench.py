@@ -247,25 +247,30 @@ def run_gpu(args) -> dict:
     iss["frac"] = iss["achieved_ops"] / iss["peak_ops"]
 
     # ---- e2e: public API, host samples in, host image out ------------------
+    # One render state and the image buffers are made once, as a renderer
+    # drawing frame after frame at one size keeps them; every frame then runs
+    # rfk_state_rewarm (the host samples uploaded, prepared, chains warmed up
+    # again, histogram cleared), bin, blur, tonemap and the image read-back.
     out_host = torch.empty((H, W, 4), dtype=torch.float16, pin_memory=True)
+    blurred = torch.empty((H, W, 4), dtype=torch.float32, device="cuda")
+    img = torch.empty((H, W, 4), dtype=torch.float16, device="cuda")
+    s2 = k.warmup(samples, (W, H), seed=99, count=WARMUP_PASSES, stream=stream)
+    tmap = lr.tonemapper()
     e2e_times = []
     e2e_passes = 0
     for i in range(args.warmup + args.steps):
         _flush_l2(flush)
         torch.cuda.synchronize()
         t0 = time.perf_counter()
-        s2 = k.warmup(samples, (W, H), seed=100 + i, count=WARMUP_PASSES, stream=stream)
+        s2.rewarm(samples, seed=100 + i, count=WARMUP_PASSES, stream=stream)
         r = k.bin(s2, bo, stream=stream)
-        blurred = torch.empty((H, W, 4), dtype=torch.float32, device="cuda")
         with torch.cuda.stream(stream):
             lr.density_blur(s2.bins(), blurred, (W, H), 9.0, 0.0, 0.5, stream=stream)
-            img = torch.empty((H, W, 4), dtype=torch.float16, device="cuda")
-            lr.tonemapper().run(blurred, img, (W, H), s2.quality, tp["gamma"], tp["brightness"], tp["vibrancy"],
-                                fmt=lr.HALF4, stream=stream)
+            tmap.run(blurred, img, (W, H), s2.quality, tp["gamma"], tp["brightness"], tp["vibrancy"], fmt=lr.HALF4,
+                     stream=stream)
             out_host.copy_(img, non_blocking=True)
         stream.synchronize()
         dt = time.perf_counter() - t0
-        del s2
         if i >= args.warmup:
             e2e_times.append(dt)
             e2e_passes += r.total_passes  # bin iterations only; the warm-up passes count as time
@@ -597,28 +602,58 @@ def _denoise_e2e(db, net, gs, td, args, w: int = 1920, h: int = 1080) -> tuple[f
     host = torch.empty((h, w, 4), dtype=torch.float16, pin_memory=True)
     times, h2d = [], 0
     n = min(len(fs), max(args.steps, 3))
+    # the flames share one structure: one render state, warmed up again per frame
+    st = k.warmup(fs[0].pack_samples(4, w, h), (w, h), seed=999, count=20)
     for i in range(n + 1):
         f = fs[i % len(fs)]
         tp = f.tonemap_params()
         samples = f.pack_samples(4, w, h)
         torch.cuda.synchronize()
         t0 = time.perf_counter()
-        st = k.warmup(samples, (w, h), seed=1000 + i, count=20)
+        st.rewarm(samples, seed=1000 + i, count=20)
         k.bin(st, lr.bailout_args(iters=0, millis=0, quality=td.LOW_SPP))
         tm.run(st.bins(), base, (w, h), st.quality, tp["gamma"], tp["brightness"], tp["vibrancy"], fmt=lr.FLOAT4)
         net.denoise(st.bins(), base, out, st.quality, fmt=lr.HALF4)
         host.copy_(out, non_blocking=True)
         torch.cuda.synchronize()
         dt = time.perf_counter() - t0
-        del st
         if i > 0:
             times.append(dt)
             h2d = int(np.asarray(samples).nbytes)
     return float(np.median(times)), h2d, int(out.numel() * out.element_size())
 
 
+def reference_cuda(spp: float = SPP) -> dict:
+    """The reference's own chaos-game kernel on this GPU: assets/kernels/refactor.cu
+    specialised for the bench genome (oracle/ref_flame.py, oracle/build_ref.py)
+    and run as flame_kernel::warmup + bin drive it (oracle/ref_run.py), at the
+    bench's size and spp; chain steps per second of its bin launch (CUDA
+    events), and the fraction of its draws its histogram kept, as written
+    (non-atomic update) and with that update made atomic."""
+    try:
+        import torch
+    except ImportError:
+        return {"unavailable": "no torch"}
+    if not torch.cuda.is_available():
+        return {"unavailable": "no GPU"}
+    from oracle import ref_run, refkernels
+
+    if not (refkernels.available("refactor_bench") and refkernels.available("catmull")):
+        return {"unavailable": "the reference's kernels were not built (oracle/build_ref.py needs the reference sources)"}
+    out = {"workload": WORKLOAD, "spp": spp}
+    for key, mod in (("as_written", "refactor_bench"), ("atomic_update", "refactor_bench_atomic")):
+        ref_run.reference_render(mod, 1, 16.0)  # load the module, warm up
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        _, info = ref_run.reference_render(mod, 2, spp, timing=(e0, e1))
+        ms = e0.elapsed_time(e1)
+        out[key] = {"iterations_per_s": info["passes"] / (ms * 1e-3), "bin_ms": ms, "kept": 1.0 - info["lost"],
+                    "quality": info["quality"]}
+    return out
+
+
 def run_reference(args) -> dict:
-    """CPU reference leg: the FP64 oracle port on all host cores."""
+    """CPU reference leg: the FP64 oracle port on all host cores; beside it,
+    the reference's own CUDA kernel timed on this GPU (`reference_cuda`)."""
     ws, rank = _dist()
     if rank != 0:
         return {}
@@ -641,6 +676,7 @@ def run_reference(args) -> dict:
         "cpu_baseline": {"value": v, "unit": "iterations/s", "cores": vals[0]["cores"], "kind": "port",
                          "sample": vals[0]["sample"]},
         "e2e": {"value": v, "unit": "iterations/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "reference_cuda": reference_cuda() if args.reference_cuda else {"unavailable": "not requested"},
     }
 
 
@@ -685,6 +721,8 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--reference-cuda", type=int, default=1,
+                    help="--impl reference: also time the reference's own CUDA kernel on the GPU (1) or not (0)")
     ap.add_argument("--workload", default="hd", choices=["hd", "anim", "hetero", "denoise"],
                     help="hd: the 1080p single-flame bench (default); anim / hetero: the batched workloads; "
                          "denoise: the learned denoiser's s/frame to 40 dB")

@@ -1,13 +1,13 @@
 """Loads the reference's own kernels (built by oracle/build_ref.py into
-oracle/_ref/) and launches them on torch CUDA tensors, for parity tests.
-Test infrastructure only."""
+oracle/_ref/) and launches them on torch CUDA tensors: the parity tests and
+the bench's reference arm run them. Test infrastructure only."""
 from __future__ import annotations
 
 import ctypes as C
 import json
 from pathlib import Path
 
-REF = Path(__file__).resolve().parent.parent / "oracle" / "_ref"
+REF = Path(__file__).resolve().parent / "_ref"
 _cudart = None
 _libs: dict = {}
 

@@ -177,16 +177,22 @@ RFK_FN float rfk_u01f(rfk_u32 u) { return (float)(u >> 8) * 5.9604644775390625e-
 
 // A chain's random stream for one pass: four words from one Philox block,
 // refilled from the next sub-counter when used up. Shifting the words keeps
-// every access at a static register index.
+// every access at a static register index. `pool` holds spare random bits
+// handed over by the caller (above a marker bit; 0 or 1 = none), which bit()
+// uses before it draws a word: the xform pick of the sorted kernels takes the
+// top 24 bits of its word and passes the low 8 on, so a variation's random
+// bit (julia) costs no Philox block.
 struct Rng {
     rfk_u32 b0, b1, b2, b3;
     rfk_u32 left;
     rfk_u32x4 ctr;
     rfk_u32 k0, k1;
+    rfk_u32 pool;
 
     RFK_FN void start(rfk_u32 stream, rfk_u32 sub, rfk_u64 pass, rfk_u32 key0, rfk_u32 key1) {
         ctr.x = stream; ctr.y = sub; ctr.z = (rfk_u32)pass; ctr.w = (rfk_u32)(pass >> 32);
         k0 = key0; k1 = key1;
+        pool = 0u;
         refill();
     }
     // As start(), but the first block is generated on the first draw: a chain
@@ -196,7 +202,10 @@ struct Rng {
         k0 = key0; k1 = key1;
         b0 = b1 = b2 = b3 = 0u;
         left = 0;
+        pool = 0u;
     }
+    // Eight spare random bits for bit().
+    RFK_FN void give_bits(rfk_u32 bits8) { pool = (bits8 & 0xFFu) | 0x100u; }
     RFK_FN void refill() {
         rfk_u32x4 r = rfk_philox(ctr, k0, k1);
         b0 = r.x; b1 = r.y; b2 = r.z; b3 = r.w; left = 4;
@@ -208,7 +217,14 @@ struct Rng {
         return r;
     }
     RFK_FN R u01() { return (R)rfk_u01f(next()); }
-    RFK_FN R bit() { return (R)((next() >> 24) & 1u); }
+    RFK_FN R bit() {
+        if (pool > 1u) {
+            const rfk_u32 r = pool & 1u;
+            pool >>= 1;
+            return (R)r;
+        }
+        return (R)((next() >> 24) & 1u);
+    }
     // Same distribution as random.h:9-14: angle 2*pi*u, radius sigma * (sum of
     // four uniforms - 2).
     RFK_FN V2 gauss(R sigma) {

@@ -336,7 +336,8 @@ __device__ __forceinline__ int rfk_step(float& x, float& y, float& c, unsigned& 
 // places in the per-warp xform counters; a warp scan of the counters gives
 // each xform's start. Only __syncwarp is needed.
 __device__ __forceinline__ void rfk_sort_chains(float4* __restrict__ region, const float4 (&v)[RFK_CPT],
-                                                const int (&k)[RFK_CPT], unsigned* __restrict__ counts) {
+                                                const int (&k)[RFK_CPT], const unsigned (&bits)[RFK_CPT],
+                                                unsigned* __restrict__ counts) {
     const unsigned lane = threadIdx.x & 31u;
     const unsigned lt = (1u << lane) - 1u;
     if (lane < RFK_NX) counts[lane] = 0u;
@@ -363,7 +364,7 @@ __device__ __forceinline__ void rfk_sort_chains(float4* __restrict__ region, con
 #pragma unroll
     for (int q = 0; q < RFK_CPT; q++) {
         const unsigned pos = __shfl_sync(0xffffffffu, start, k[q]) + off[q];
-        region[pos] = make_float4(v[q].x, v[q].y, v[q].z, __int_as_float(k[q]));
+        region[pos] = make_float4(v[q].x, v[q].y, v[q].z, __int_as_float(k[q] | (int)(bits[q] << 8)));
     }
     __syncwarp();
 }
@@ -382,8 +383,8 @@ __device__ __forceinline__ void rfk_sort_chains(float4* __restrict__ region, con
 // holds thread t's round-q chain, so a warp's round covers 32 consecutive
 // slots of one xform run except at run ends.
 __device__ __forceinline__ void rfk_block_sort(float4* __restrict__ chains, const float4 (&v)[RFK_CPT],
-                                               const int (&k)[RFK_CPT], unsigned* __restrict__ counts,
-                                               unsigned* __restrict__ next) {
+                                               const int (&k)[RFK_CPT], const unsigned (&bits)[RFK_CPT],
+                                               unsigned* __restrict__ counts, unsigned* __restrict__ next) {
     const unsigned lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
     const unsigned lt = (1u << lane) - 1u;
     unsigned off[RFK_CPT];
@@ -419,7 +420,7 @@ __device__ __forceinline__ void rfk_block_sort(float4* __restrict__ chains, cons
 #pragma unroll
     for (int q = 0; q < RFK_CPT; q++) {
         const unsigned pos = __shfl_sync(0xffffffffu, start, k[q]) + off[q];
-        chains[pos] = make_float4(v[q].x, v[q].y, v[q].z, __int_as_float(k[q]));
+        chains[pos] = make_float4(v[q].x, v[q].y, v[q].z, __int_as_float(k[q] | (int)(bits[q] << 8)));
     }
     __syncthreads();
 }
@@ -488,8 +489,9 @@ __device__ __forceinline__ void rfk_cache_add(rfk_cache& cc, float4* __restrict_
 // pixel and check interval; every other draw is one red.v4 after a single
 // 16-byte table load, with no warp-wide matching of pixels.
 //   discovery  in the first RFK_DISC_PASSES passes of every check interval,
-//              the draws of slot 0 of each thread are counted per pixel in a
-//              hash table (linear probing, at most RFK_DISC_PROBES places);
+//              the draws of one chain in RFK_CPT (RFK_DISC below) are counted
+//              per pixel in a hash table (linear probing, at most
+//              RFK_DISC_PROBES places);
 //   rebuild    after those passes (all threads, between barriers): the old
 //              sums are flushed, and every pixel counted RFK_HOT_MIN times or
 //              more becomes hot (at most RFK_HOT_MAX, the first two free ways
@@ -768,11 +770,14 @@ __device__ __forceinline__ void rfk_store_chains(const rfk_pass_smem& sm, const 
 #define RFK_CACHE_ARG
 #endif
 
-// Flush 4: the discovery passes of a check interval sample the draws of slot
-// 0; after the last of them the block rebuilds its hot-pixel table. Both
-// depend only on the pass number within the interval (block-uniform).
+// Flush 4: the discovery passes of a check interval sample one chain in
+// RFK_CPT, spread over the whole sorted chain order (slot q of the threads
+// whose index is q modulo RFK_CPT: the sort puts the chains of the first
+// xforms in the low slots, so one slot alone would see only those xforms'
+// pixels); after the last of them the block rebuilds its hot-pixel table.
+// Both depend only on the pass number within the interval (block-uniform).
 #if RFK_FLUSH == 4
-#define RFK_DISC(it, q) ((it) < RFK_DISC_PASSES && (q) == 0)
+#define RFK_DISC(it, q) ((it) < RFK_DISC_PASSES && threadIdx.x % RFK_CPT == (unsigned)(q))
 #define RFK_HOT_PASS_END(it, bins) \
     if ((it) + 1 == RFK_DISC_PASSES) rfk_hot_rebuild(sm.hot, (bins));
 #else
@@ -803,15 +808,20 @@ __device__ __forceinline__ void rfk_pick_sort(rfk_pass_smem& sm, const float* P,
     pr.start_lazy(lane_stream, call_id, pass, seed, salt ^ 0x9E3779B9u);
     float4 v[RFK_CPT];
     int kk[RFK_CPT];
+    unsigned bits[RFK_CPT];
 #pragma unroll
     for (int q = 0; q < RFK_CPT; q++) {
         v[q] = sm.chains[rfk_slot(q)];
-        kk[q] = rfk_pick(pr.u01(), P, (unsigned)__float_as_int(v[q].w));
+        const rfk_u32 u = pr.next();
+        // the pick takes the top 24 bits; the low 8 go with the chain to its
+        // move (Rng::give_bits)
+        kk[q] = rfk_pick(rfk_u01f(u), P, (unsigned)__float_as_int(v[q].w));
+        bits[q] = u & 0xFFu;
     }
 #if RFK_SORT == 2
-    rfk_block_sort(sm.chains, v, kk, sm.counts[pass & 1], sm.counts[(pass + 1) & 1]);
+    rfk_block_sort(sm.chains, v, kk, bits, sm.counts[pass & 1], sm.counts[(pass + 1) & 1]);
 #else
-    rfk_sort_chains(sm.chains + (threadIdx.x & ~31u) * RFK_CPT, v, kk, sm.counts[threadIdx.x >> 5]);
+    rfk_sort_chains(sm.chains + (threadIdx.x & ~31u) * RFK_CPT, v, kk, bits, sm.counts[threadIdx.x >> 5]);
 #endif
 #else
     (void)sm; (void)P; (void)lane_stream; (void)call_id; (void)pass; (void)seed; (void)salt;
@@ -832,8 +842,11 @@ __device__ __forceinline__ void rfk_move_slot(int q, unsigned chain, rfk_pass_sm
     int idx;
     Rng rng;
 #if RFK_SORT
-    // the sort left this slot's pick in the last-xform field
+    // the sort left this slot's pick in the last-xform field, with 8 spare
+    // random bits of the pick's word above it
     rng.start_lazy(chain, call_id, pass, seed, salt);
+    rng.give_bits(last >> 8);
+    last &= 0xFFu;
     idx = rfk_move((int)last, x, y, c, rng, P, w, h, v, hit);
 #else
     rng.start(chain, call_id, pass, seed, salt);

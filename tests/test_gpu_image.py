@@ -11,7 +11,7 @@ torch = pytest.importorskip("torch")
 from oracle import oracle as orc
 from refraktor_gb300 import librefrakt as lr
 
-from . import refkernels
+from oracle import refkernels
 
 pytestmark = pytest.mark.gpu
 

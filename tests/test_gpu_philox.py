@@ -12,7 +12,7 @@ torch = pytest.importorskip("torch")
 
 from oracle.build_ref import compile_module
 from refraktor_gb300 import build
-from tests import refkernels
+from oracle import refkernels
 from tests.test_cpu_philox import KAT, philox_py, random_cases
 
 pytestmark = pytest.mark.gpu

@@ -28,9 +28,24 @@ pytestmark = pytest.mark.gpu
 N = 1024
 SEED = 5
 
-# variation -> (median forward ulp bound, fraction of points within 4 ulps backward)
-BOUNDED = {"polar": (2.0, 0.99), "handkerchief": (2.0, 0.99), "disc": (2.0, 0.99), "heart": (2.0, 0.99),
-           "diamond": (2.0, 0.99), "spiral": (2.0, 0.95), "ex": (2.0, 0.97), "cosine": (1.0, 0.999)}
+# variation -> (median forward ulp bound, fraction of points within 4 ulps
+# backward), measured on GB300 (1024 points). Beside the angle-composing
+# variations of the classic set: popcorn's tan(3y) amplifies the input's
+# rounding near its poles; cross cancels in x^2 - y^2 near the
+# diagonals; gaussian_blur sums four FP32 uniforms and subtracts 2 (the
+# reference's Irwin-Hall gaussian), which cancels near 0; curl, log,
+# juliascope and rectangles compose a rounded intermediate (a quotient, a
+# logarithm's argument, a power, a floor) with the output.
+BOUNDED = {"polar": (2.0, 0.985), "handkerchief": (2.0, 0.99), "disc": (2.0, 0.99), "heart": (2.0, 0.99),
+           "diamond": (2.0, 0.99), "spiral": (2.0, 0.95), "ex": (2.0, 0.97), "cosine": (1.0, 0.999),
+           "cross": (1.0, 0.90), "gaussian_blur": (2.0, 0.75), "curl": (1.0, 0.995), "log": (1.0, 0.995),
+           "juliascope": (1.0, 0.98), "rectangles": (1.0, 0.995), "popcorn": (1.0, 0.85)}
+
+# Variations that read the vlink's affine offsets (aff.c, aff.f): they get
+# offsets (0.25, -0.375) instead of the identity's zeros (waves divides by
+# their squares), with inputs on a 2^-12 grid so that the affine's additions
+# are exact in FP32 and the variation sees the same point in both precisions.
+AFF_OFFSET = {"fan": (0.25, -0.375), "popcorn": (0.25, -0.375), "rings": (0.25, -0.375), "waves": (0.25, -0.375)}
 
 
 def _flame(names, params):
@@ -46,8 +61,9 @@ def _flame(names, params):
             # some of them degenerate)
             entry = {"weight": w, "parameters": {
                 p: float((d if d is not None else rng.uniform(0.3, 1.0)) * rng.uniform(0.6, 1.4)) for p, d in ps}}
+        c, f = AFF_OFFSET.get(name, (0.0, 0.0))
         xfs.append({"weight": 1.0, "color": float(rng.uniform()), "color_speed": 0.5, "opacity": 1.0,
-                    "vchain": [{"transform": [1.0, 0.0, 0.0, 1.0, 0.0, 0.0], "mod_x": 0, "mod_y": 0, "mod_scale": 1,
+                    "vchain": [{"transform": [1.0, 0.0, 0.0, 1.0, c, f], "mod_x": 0, "mod_y": 0, "mod_scale": 1,
                                 "mod_rotate": 0, "variations": {name: entry}}]})
     g["xforms"] = xfs
     return g
@@ -79,6 +95,9 @@ def test_variation_matches_fp64_twin(setup, xi):
     name = names[xi]
     rng = np.random.default_rng(1000 + xi)
     pts = np.stack([rng.uniform(-1.5, 1.5, N), rng.uniform(-1.5, 1.5, N), rng.uniform(0, 1, N)], 1).astype(np.float32)
+    c, fo = AFF_OFFSET.get(name, (0.0, 0.0))
+    if name in AFF_OFFSET:
+        pts[:, :2] = np.round(pts[:, :2] * 4096.0) / 4096.0
     out = k.apply_xform(prep, xi, pts, seed=SEED).astype(np.float64)
     P = prep[:f.size_reals()].astype(np.float64)
     idx = np.arange(N)
@@ -91,7 +110,9 @@ def test_variation_matches_fp64_twin(setup, xi):
     if bad.size:
         # backward: the nearest FP64 result over inputs within 2 ulps per coordinate
         q0 = pts[bad].astype(np.float64)
-        sx, sy = np.spacing(pts[bad, 0]).astype(np.float64), np.spacing(pts[bad, 1]).astype(np.float64)
+        # ulps of the point the variation sees (after the affine's exact offsets)
+        sx = np.spacing((pts[bad, 0] + np.float32(c)).astype(np.float32)).astype(np.float64)
+        sy = np.spacing((pts[bad, 1] + np.float32(fo)).astype(np.float32)).astype(np.float64)
         qs, ids = [], []
         for i in range(-2, 3):
             for j in range(-2, 3):
