@@ -45,14 +45,13 @@ WORKLOAD = "plain 1080p single flame: 1920x1080, 1024 spp, 8 xforms + final xfor
 
 # dram__bytes_read.sum + dram__bytes_write.sum of one 1024-spp rfk_bin launch of
 # this workload at the bench's launch shape (608 x 256, 8 chains per thread,
-# flush 1, block sort; one ncu pass over the --ncu-case launch at 1024 spp)
-BIN_DRAM_BYTES_PER_LAUNCH = 46.70e6 + 148.53e6
-# smsp__inst_executed.sum / chain steps of one 16-spp rfk_bin launch of this
-# workload at the bench's launch shape (608 x 256, 8 chains per thread, flush
-# 1, block sort): 451.1 M warp instructions for 36.77 M chain steps (ncu over
-# the --ncu-case launch); each SM sub-partition issues one warp instruction per
-# clock
-BIN_WARP_INST_PER_ITER = 451.10e6 / 36.77e6
+# flush 4, block sort, 4 blocks per SM; one ncu pass over the --ncu-case launch
+# at 1024 spp)
+BIN_DRAM_BYTES_PER_LAUNCH = 46.795264e6 + 12.903424e6
+# smsp__inst_executed.sum / chain steps of the same 1024-spp launch: 23.157 G
+# warp instructions for 2.168 G chain steps; each SM sub-partition issues one
+# warp instruction per clock
+BIN_WARP_INST_PER_ITER = 23156553057 / 2168324096
 # dram__bytes_read.sum + dram__bytes_write.sum of one rfk_bin_batch launch of
 # each batched workload (ncu, one pass over the bench's own batch launch);
 # None until captured

@@ -185,7 +185,7 @@ def evaluate_with_fallback(db, net, genomes, w: int, h: int, seed: int = 7, kern
         del st_ref
         st, t_warm = timed(lambda: k.warmup(samples, (w, h), seed=seed + 2 * i, count=20, stream=stream))
         _, t_tm = timed(lambda: tm.run(st.bins(), img, (w, h), 1.0, *tmargs, fmt=lr.FLOAT4, stream=stream))
-        spp, t_bin, psnrs, den_db, t_den = [0.0], [0.0], [], None, None
+        spp, t_bin, psnrs, den_db, t_den, den64_db, den_vs_plain = [0.0], [0.0], [], None, None, None, None
         for c in FALLBACK_CHECKPOINTS:
             _, dt = timed(lambda: k.bin(st, lr.bailout_args(iters=0, millis=0, quality=c - st.quality), stream=stream))
             spp.append(st.quality)
@@ -196,12 +196,19 @@ def evaluate_with_fallback(db, net, genomes, w: int, h: int, seed: int = 7, kern
             if c == FALLBACK_CHECKPOINTS[0]:
                 _, t_den = timed(lambda: net.denoise(st.bins(), img, den, st.quality, stream=stream))
                 den_db = dn.psnr(den, ref)
-            if psnrs[-1] >= 40.0:
+                # no-reference: how far the U-Net moved the plain image
+                den_vs_plain = dn.psnr(den, img)
+            if c == 64:
+                net.denoise(st.bins(), img, den, st.quality, stream=stream)
+                den64_db = dn.psnr(den, ref)
+            if psnrs[-1] >= 40.0 and c >= 64:
                 break
         row = {"psnr_denoised": den_db, "psnr_plain": psnrs, "spp": spp[1:], "t_warmup": t_warm, "t_tonemap": t_tm,
-               "t_unet": t_den, "t_bin_32": t_bin[1]}
-        if psnrs[-1] >= 40.0:
-            j = len(psnrs) - 1
+               "t_unet": t_den, "t_bin_32": t_bin[1], "psnr_denoised_64": den64_db,
+               "psnr_denoised_vs_plain_32": den_vs_plain, "t_bin": t_bin[1:]}
+        if max(psnrs) >= 40.0:
+            # the first checkpoint at or above 40 dB
+            j = next(i for i, v in enumerate(psnrs) if v >= 40.0)
             if j == 0:
                 s40, tb40 = spp[1], t_bin[1]
             else:

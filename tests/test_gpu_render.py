@@ -13,6 +13,7 @@ torch = pytest.importorskip("torch")
 from oracle import oracle as orc
 from refraktor_gb300 import librefrakt as lr
 from refraktor_gb300 import synthetic as syn
+from tests import fp32_ideal as fi
 from tests.pick_tables import alias_distribution
 
 pytestmark = pytest.mark.gpu
@@ -225,12 +226,16 @@ def test_rewarm_reuses_the_state(db, comp):
     np.testing.assert_array_equal(a[..., 3] > 0, b[..., 3] > 0)
     np.testing.assert_allclose(a, b, rtol=1e-5, atol=1e-6)
     # without clearing, the next render draws on top: the same draws again
-    # (each added to a sum that already holds the first render's)
+    # (each added to a sum that already holds the first render's). Every add
+    # into a hot pixel now rounds at that pixel's doubled magnitude, and the
+    # opacities are nearly constant, so the rounding errors add up with one
+    # sign (measured 2e-4 of the total alpha); 1e-3 still separates the kept
+    # histogram (2x the sums) from a cleared one (1x).
     st.rewarm(s2, seed=9, count=20, clear=False)
     r2 = k.bin(st, lr.bailout_args(iters=4, millis=0, quality=0))
     assert r2.draw_count == rf.draw_count
     c2 = st.bins().cpu().numpy().astype(np.float64)
-    np.testing.assert_allclose(c2.sum(axis=(0, 1)), 2 * b.astype(np.float64).sum(axis=(0, 1)), rtol=1e-4)
+    np.testing.assert_allclose(c2.sum(axis=(0, 1)), 2 * b.astype(np.float64).sum(axis=(0, 1)), rtol=1e-3)
     np.testing.assert_array_equal(c2[..., 3] > 0, b[..., 3] > 0)
     # not while a bin call is pending
     k.bin_async(st, lr.bailout_args(iters=5, millis=0, quality=0))
@@ -361,14 +366,12 @@ def test_affine_step_exact_fma(db, comp):
 # Variations whose formula composes FP32-rounded angles of magnitude up to 2 pi
 # with the radius (atan +- sqrt, sqrt * atan) or cancels (spiral: cosa + sin r,
 # polar: sqrt - 1): the rounding of those intermediate arguments alone exceeds
-# 4 ulp of the output for some inputs, so they are held to the distribution
-# bounds below instead of the per-point bound.
-# Measured on GB300 (2048 points, |p| <= 1.5): forward-error median / 90th
-# percentile bounds in ulp, and the fraction of points whose backward error
-# is within 4 ulp.
-ANGLE_COMPOSED = {"polar": (2.0, 4.0, 0.99), "handkerchief": (2.0, 4.0, 0.99), "disc": (2.0, 4.0, 0.99),
-                  "heart": (2.0, 4.0, 0.99), "diamond": (2.0, 4.0, 0.99), "spiral": (2.0, 4.0, 0.95),
-                  "ex": (2.0, 8.0, 0.97)}
+# 4 ulp of the output for some inputs - even with every FP32 operation
+# correctly rounded (tests/test_cpu_fp32_bounds.py) - so they are held to the
+# measured distribution bounds of tests/fp32_ideal.py: forward-error median /
+# 90th percentile in ulp, and the fraction of points whose backward error is
+# within 4 ulp (GB300, 2048 points, |p| <= 1.5).
+ANGLE_COMPOSED = fi.ANGLE_COMPOSED
 
 
 @pytest.mark.parametrize("name", DETERMINISTIC)
