@@ -1043,10 +1043,18 @@ rfk_status rfk_autotune(const rfk_db* db, const rfk_flame* f, const double* samp
                 return;
             }
         }
+        // Only strategies that add aggregated sums (flush 1, 2, 4) are
+        // candidates. With one red.v4 per draw (flush 0, 3) a pixel that
+        // reaches 2^24 keeps that value: adding an opacity of 1 is a tie that
+        // rounds back to the even 2^24, and smaller opacities round away
+        // entirely, so a long render of a flame with a few hot pixels loses
+        // most of their draws. The 256-pass timing launches cannot tell
+        // whether the caller's render will get there; callers that know
+        // their pixels stay below 2^24 draws may still compile flush 0.
         struct cand { int block, cpt, flush, sort, minb; };
         const cand cands[] = {{256, 8, 4, 2, 4}, {256, 4, 4, 2, 5}, {128, 8, 4, 2, 8}, {256, 4, 4, 1, 5},
                               {128, 8, 1, 2, 8}, {256, 8, 1, 2, 4}, {256, 4, 1, 2, 4}, {256, 2, 1, 2, 6},
-                              {128, 4, 1, 2, 12}, {256, 4, 2, 2, 5}, {256, 4, 0, 2, 5}, {256, 4, 1, 1, 5}};
+                              {128, 4, 1, 2, 12}, {256, 4, 2, 2, 5}, {256, 4, 1, 1, 5}};
         double best_rate = -1.0, worst_rate = 1e300;
         int n = 0;
         for (const cand& c : cands) {

@@ -27,6 +27,13 @@ import numpy as np
 ANGLE_COMPOSED = {"polar": (2.0, 4.0, 0.99), "handkerchief": (2.0, 4.0, 0.99), "disc": (2.0, 4.0, 0.99),
                   "diamond": (2.0, 4.0, 0.99), "spiral": (2.0, 4.0, 0.95), "ex": (2.0, 8.0, 0.97)}
 
+# Variations held to the per-point backward bound whose forward error at the
+# exact input is above 4 ulp at more than 1% of the points even when correctly
+# rounded (the formula's conditioning, not its rounding: heart's sin(atan *
+# sqrt) moves by more than 4 ulp of the output between neighbouring FP32
+# inputs), with the forward fraction the GPU test requires instead of 0.99.
+FORWARD_WITHIN_4 = {"heart": 0.97}
+
 IDEAL = ("polar", "handkerchief", "heart", "disc", "spiral", "diamond", "ex")
 
 

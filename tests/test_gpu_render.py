@@ -418,7 +418,8 @@ def test_single_map_within_4_ulp(db, comp, name):
         assert np.mean(best[ok] <= 4) >= frac, (name, np.mean(best[ok] <= 4))
     else:
         assert np.all(best[ok] <= 4), (name, float(best[ok].max()))
-        assert np.median(fwd[ok]) <= 1.0 and np.mean(fwd[ok] <= 4) >= 0.99, (name, np.percentile(fwd[ok], [50, 99]))
+        frac4 = fi.FORWARD_WITHIN_4.get(name, 0.99)
+        assert np.median(fwd[ok]) <= 1.0 and np.mean(fwd[ok] <= 4) >= frac4, (name, np.percentile(fwd[ok], [50, 99]))
     np.testing.assert_allclose(out[:, 2], ref[:, 2], rtol=1e-6, atol=1e-7)  # colour blend
     assert np.all(out[:, 3] == 1.0)
 
@@ -578,13 +579,49 @@ def test_sort_and_flush_variants_agree(db, comp, sort, flush):
     assert np.abs(a - c).sum() < 1.25 * floor + 0.002, (np.abs(a - c).sum(), floor)
 
 
+@pytest.mark.parametrize("flush", [0, 1, 2, 4])
+def test_hot_pixel_past_2_24_draws(db, comp, flush):
+    """A flame whose one xform (x/2, y/2) pulls every chain onto the origin,
+    framed at the centre of a 64 x 64 image, so that the warmed-up chains'
+    draws all land on the (jittered) centre pixels, opacity 1, about 200 M
+    draws: each of the few hot pixels passes 2^24 draws. With one red.v4 per
+    draw (flush 0) a pixel that reaches 2^24 stays there - 2^24 + 1 is a tie
+    that rounds to the even 2^24 - so the histogram loses most of the draws;
+    this is why the autotuner never picks it. The aggregating strategies add
+    warp or block sums, which keep counting: the density sum equals the draw
+    count."""
+    g = syn.plain_flame(3)
+    g.update(center_x=0.0, center_y=0.0, scale=0.5, rotate=0.0)
+    g["xforms"] = [{"weight": 1.0, "color": 0.5, "color_speed": 0.5, "opacity": 1.0,
+                    "vchain": [{"transform": [0.5, 0.0, 0.0, 0.5, 0.0, 0.0], "mod_x": 0, "mod_y": 0, "mod_scale": 1,
+                                "mod_rotate": 0, "variations": {"linear": 1.0}}]}]
+    g.pop("final_xform", None)
+    f = lr.flame.from_json(db, g)
+    k = comp.get_flame_kernel(db, f, sort=2, flush=flush)
+    w = h = 64
+    chains = k.info["grid"] * k.info["block"] * k.info["chains_per_thread"]
+    passes = int(np.ceil(2.0e8 / chains))
+    st = k.warmup(f.pack_samples(4, w, h), (w, h), seed=4, count=40)
+    r = k.bin(st, lr.bailout_args(iters=passes, millis=0, quality=0))
+    assert r.draw_count == passes * chains  # every step draws, inside the image
+    dens = st.bins().cpu().numpy().astype(np.float64)[..., 3]
+    assert dens.max() > 2.0 ** 24 or flush == 0
+    if flush == 0:
+        assert dens.max() == 2.0 ** 24
+        assert dens.sum() < 0.9 * r.draw_count
+    else:
+        assert abs(dens.sum() - r.draw_count) <= 1e-5 * r.draw_count, (dens.sum(), r.draw_count)
+
+
 def test_autotune_picks_a_tested_variant_and_caches(db, comp):
     """rfk_autotune: its pick is one of the (sort, flush) variants that
     test_sort_and_flush_variants_agree renders against the default, with a
     launch shape that compiles and renders; a second call with the same flame,
     samples and size is answered from the cache (no candidate runs, same
     options), and another size is tuned again."""
-    tested = {(2, 0), (2, 1), (2, 2), (2, 3), (2, 4), (1, 2), (1, 4), (-1, 1), (-1, 4)}
+    # aggregating strategies only: one red per draw stops counting at 2^24
+    # (test_hot_pixel_past_2_24_draws)
+    tested = {(2, 1), (2, 2), (2, 4), (1, 2), (1, 4), (-1, 1), (-1, 4)}
     f = lr.flame.from_json(db, syn.hd_flame(6))
     w, h = 320, 180
     samples = f.pack_samples(4, w, h)
