@@ -74,6 +74,15 @@ struct rfk_batch {
     size_t total_px = 0, img_bytes = 0;
     uint64_t nitems = 0;
     unsigned naff = 0;
+    // Runs of samples [first, first + count) that fix_rotation unwraps as one
+    // spline: consecutive samples j - 1 and j are in one run when a unit's
+    // segment uses both (its knots seg .. seg + 3). Unwrapping across samples
+    // that no segment joins (one independent flame after another) would add
+    // multiples of 2 pi to the later flames' angles, which then reach FP32
+    // with a coarser rounding than the same flame rendered alone; restarting
+    // keeps every independent flame's prepared parameters bit-identical to the
+    // single-flame path's.
+    std::vector<std::pair<unsigned, unsigned>> rot_runs;
 
     double* d_samples = nullptr;
     float4* d_coeff = nullptr;
@@ -121,10 +130,12 @@ struct rfk_batch {
         cuda_check(cudaMemcpyAsync(d_call, h_call, sizeof(unsigned), cudaMemcpyHostToDevice, s), "H2D run id");
         cuda_check(cudaMemcpyAsync(d_samples, h_samples, nsamples * sample_size * sizeof(double), cudaMemcpyHostToDevice, s),
                    "H2D samples");
-        cuda_check(rfk_launch_fix_rotation(d_samples, (unsigned)nsamples, (unsigned)sample_size, (unsigned)k->gen.size_reals,
-                                           d_aff, naff, s),
-                   "fix_rotation");
-        n++;
+        for (const auto& r : rot_runs) {
+            cuda_check(rfk_launch_fix_rotation(d_samples + (size_t)r.first * sample_size, r.second, (unsigned)sample_size,
+                                               (unsigned)k->gen.size_reals, d_aff, naff, s),
+                       "fix_rotation");
+            n++;
+        }
         const unsigned nseg = (unsigned)(nsamples - 3);
         cuda_check(rfk_launch_catmull(d_samples, (unsigned)sample_size, nseg, d_coeff, s), "catmull");
         n++;
@@ -233,6 +244,21 @@ rfk_status rfk_batch_create(rfk_kernel* k, const rfk_batch_unit* units, size_t n
         const unsigned nseg = (unsigned)(nsamples - 3);
         b->nsamples = nsamples;
         b->sample_size = b->k->gen.size_reals + rfk::palette_reals;
+        {
+            // joined[j]: samples j - 1 and j belong to one unit's segment
+            std::vector<char> joined(nsamples, 0);
+            for (size_t u = 0; u < nunits; u++) {
+                const size_t sg = units[u].segment;
+                if (sg >= nseg) continue;  // rejected below
+                for (size_t j = sg + 1; j <= sg + 3; j++) joined[j] = 1;
+            }
+            unsigned first = 0;
+            for (unsigned j = 1; j <= (unsigned)nsamples; j++)
+                if (j == (unsigned)nsamples || !joined[j]) {
+                    b->rot_runs.emplace_back(first, j - first);
+                    first = j;
+                }
+        }
 
         // queue: items per unit from the least number of chain steps that can
         // reach the target (every step a full-opacity draw), times item_factor

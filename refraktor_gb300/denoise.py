@@ -201,27 +201,34 @@ class train_report:
     ms_per_step: float
 
 
-def train(net: denoiser, bins, base, targets, spp: float, steps: int, batch: int = 16, lr_: float = 1e-3,
+def train(net: denoiser, bins, base, targets, spp, steps: int, batch: int = 16, lr_: float = 1e-3,
           val: Optional[tuple] = None, seed: int = 0, log=None, augment: bool = True) -> train_report:
     """Adam on random mini-batches of the (N, h, w, 4) training tensors,
-    randomly mirrored; cosine-decayed learning rate. val: (bins, base, targets)."""
+    randomly mirrored; cosine-decayed learning rate. val: (bins, base,
+    targets). Several input sample counts: `bins`, `base` and `spp` are lists
+    (one histogram / image set per spp, of the same flames and targets), and
+    the steps take them in turn, so that the network's log-spp input channel
+    sees every count; val then holds one (bins, base) per spp and the
+    validation loss is their mean."""
     import torch
 
+    sets = list(zip(bins, base, spp)) if isinstance(spp, (list, tuple)) else [(bins, base, spp)]
     g = torch.Generator(device="cpu").manual_seed(seed)
-    n = bins.shape[0]
+    n = sets[0][0].shape[0]
     losses = []
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     for s in range(steps):
+        sb, sbase, sspp = sets[s % len(sets)]
         idx = torch.randint(0, n, (batch,), generator=g).cuda()
         lr_s = lr_ * 0.5 * (1.0 + np.cos(np.pi * s / max(steps, 1)))
-        b, bb, tt = bins.index_select(0, idx), base.index_select(0, idx), targets.index_select(0, idx)
+        b, bb, tt = sb.index_select(0, idx), sbase.index_select(0, idx), targets.index_select(0, idx)
         if augment:
             # mirror images: the chaos game's statistics do not depend on orientation
             flips = [d for d, bit in ((1, 1), (2, 2)) if int(torch.randint(0, 4, (1,), generator=g)) & bit]
             if flips:
                 b, bb, tt = b.flip(flips), bb.flip(flips), tt.flip(flips)
-        l = net.train_step(b.contiguous(), bb.contiguous(), spp, tt.contiguous(), max(lr_s, lr_ * 0.02))
+        l = net.train_step(b.contiguous(), bb.contiguous(), sspp, tt.contiguous(), max(lr_s, lr_ * 0.02))
         losses.append(l)
         if log and (s % 100 == 0 or s == steps - 1):
             log(f"step {s} loss {l:.6f}")
@@ -229,9 +236,10 @@ def train(net: denoiser, bins, base, targets, spp: float, steps: int, batch: int
     dt = time.perf_counter() - t0
     vl = float("nan")
     if val is not None:
-        vb, vbase, vt = val
-        vl = float(np.mean([net.loss(vb[i:i + 4].contiguous(), vbase[i:i + 4].contiguous(), spp, vt[i:i + 4].contiguous())
-                            for i in range(0, vb.shape[0], 4)]))
+        vt = val[2]
+        vsets = list(zip(val[0], val[1], spp)) if isinstance(spp, (list, tuple)) else [(val[0], val[1], spp)]
+        vl = float(np.mean([net.loss(vb[i:i + 4].contiguous(), vbase[i:i + 4].contiguous(), vs, vt[i:i + 4].contiguous())
+                            for vb, vbase, vs in vsets for i in range(0, vb.shape[0], 4)]))
     return train_report(steps, dt, losses[0], float(np.mean(losses[-20:])), vl, 1e3 * dt / max(steps, 1))
 
 

@@ -5,8 +5,10 @@ against the plain path (the learned-denoiser workload):
                (8 xforms, Dirichlet(1) weights, final xform, 1-3 variations
                each from the 14-variation set), visibility-rejected and framed
                at 512 x 512; input: the 32-spp histogram and its tonemapped
-               image, target: the tonemapped 4096-spp render; Adam, lr 1e-3
-               (cosine decay), batch 16, random mirroring
+               image, and in turn the 64-spp ones (--input-spp; the network's
+               log-spp channel tells them apart), target: the tonemapped
+               4096-spp render; Adam, lr 1e-3 (cosine decay), batch 16,
+               random mirroring
   evaluation   `--eval` held-out seeded flames at 1920 x 1080: the plain path
                renders to 32, 64, ..., 4096 spp (one progressive render), the
                denoised path denoises its 32-spp histogram; both are scored by
@@ -143,10 +145,13 @@ def evaluate_with_fallback(db, net, genomes, w: int, h: int, seed: int = 7, kern
       plain     warm-up + bin to the spp where the PSNR against an independent
                 4096-spp render first reaches 40 dB (interpolated on log2 spp
                 between checkpoints, the bin time likewise) + one tonemap;
-      denoised  warm-up + bin to 32 spp + tonemap + U-Net; a frame whose
-                denoised PSNR stays below 40 dB then continues the plain render
-                from its 32 spp to the plain path's 40 dB spp and tonemaps
-                again, and pays that time too.
+      denoised  a cascade, each stage paid in full: warm-up + bin to 32 spp
+                + tonemap + U-Net; a frame still below 40 dB continues its
+                render to 64 spp and tonemaps (done if the plain image reached
+                40 dB by 64 spp), else runs the U-Net again on the 64-spp
+                histogram; a frame below 40 dB after that continues the plain
+                render to the plain path's 40 dB spp and tonemaps again.
+      32 only   the same without the 64-spp stage (keys *_32_only).
     Flames whose plain render stays below 40 dB at 4096 spp have no plain time
     and are left out of both means (counted in `plain_never_reaches`)."""
     import torch
@@ -186,6 +191,7 @@ def evaluate_with_fallback(db, net, genomes, w: int, h: int, seed: int = 7, kern
         st, t_warm = timed(lambda: k.warmup(samples, (w, h), seed=seed + 2 * i, count=20, stream=stream))
         _, t_tm = timed(lambda: tm.run(st.bins(), img, (w, h), 1.0, *tmargs, fmt=lr.FLOAT4, stream=stream))
         spp, t_bin, psnrs, den_db, t_den, den64_db, den_vs_plain = [0.0], [0.0], [], None, None, None, None
+        t_den64 = None
         for c in FALLBACK_CHECKPOINTS:
             _, dt = timed(lambda: k.bin(st, lr.bailout_args(iters=0, millis=0, quality=c - st.quality), stream=stream))
             spp.append(st.quality)
@@ -199,7 +205,7 @@ def evaluate_with_fallback(db, net, genomes, w: int, h: int, seed: int = 7, kern
                 # no-reference: how far the U-Net moved the plain image
                 den_vs_plain = dn.psnr(den, img)
             if c == 64:
-                net.denoise(st.bins(), img, den, st.quality, stream=stream)
+                _, t_den64 = timed(lambda: net.denoise(st.bins(), img, den, st.quality, stream=stream))
                 den64_db = dn.psnr(den, ref)
             if psnrs[-1] >= 40.0 and c >= 64:
                 break
@@ -218,22 +224,39 @@ def evaluate_with_fallback(db, net, genomes, w: int, h: int, seed: int = 7, kern
                 tb40 = t_bin[j] + fr * (t_bin[j + 1] - t_bin[j])
             plain = t_warm + tb40 + t_tm
             dpath = t_warm + t_bin[1] + t_tm + t_den
+            casc = dpath
             if den_db < 40.0:
                 dpath += max(tb40 - t_bin[1], 0.0) + t_tm
-            row.update(spp_to_40db=s40, plain_s=plain, denoised_s=dpath)
+                # cascade: at 64 spp the plain image is done if it reached 40
+                # dB by then, else the U-Net runs again; then the plain render
+                i64 = FALLBACK_CHECKPOINTS.index(64) + 1
+                if s40 <= 64.0:
+                    casc += max(tb40 - t_bin[1], 0.0) + t_tm
+                else:
+                    casc += t_bin[i64] - t_bin[1] + t_tm + t_den64
+                    if den64_db < 40.0:
+                        casc += max(tb40 - t_bin[i64], 0.0) + t_tm
+            row.update(spp_to_40db=s40, plain_s=plain, denoised_s=dpath, cascade_s=casc)
         rows.append(row)
         del st
     ok = [r for r in rows if "plain_s" in r]
     plain = np.array([r["plain_s"] for r in ok])
     dpath = np.array([r["denoised_s"] for r in ok])
+    casc = np.array([r["cascade_s"] for r in ok])
     pden = np.array([r["psnr_denoised"] for r in rows])
+    pden64 = np.array([r["psnr_denoised_64"] for r in rows])
     out = {
         "flames": len(rows), "width": w, "height": h, "plain_never_reaches": len(rows) - len(ok),
         "s_per_frame_to_40db_plain": float(plain.mean()) if ok else None,
-        "s_per_frame_to_40db_denoised": float(dpath.mean()) if ok else None,
-        "speedup": float(plain.mean() / dpath.mean()) if ok else None,
-        "speedup_per_flame_median": float(np.median(plain / dpath)) if ok else None,
+        "s_per_frame_to_40db_denoised": float(casc.mean()) if ok else None,
+        "speedup": float(plain.mean() / casc.mean()) if ok else None,
+        "speedup_per_flame_median": float(np.median(plain / casc)) if ok else None,
+        "s_per_frame_to_40db_denoised_32_only": float(dpath.mean()) if ok else None,
+        "speedup_32_only": float(plain.mean() / dpath.mean()) if ok else None,
         "denoised_reaches_40db": float((pden >= 40.0).mean()),
+        "denoised_64_reaches_40db": float((pden64 >= 40.0).mean()),
+        "cascade_reaches_40db_by_64spp": float(np.mean([(a >= 40.0) or (b >= 40.0) or r.get("spp_to_40db", 1e9) <= 64.0
+                                                        for a, b, r in zip(pden, pden64, rows)])),
         "denoised_psnr_db_mean": float(pden.mean()), "denoised_psnr_db_median": float(np.median(pden)),
         "plain_psnr_db_32spp_mean": float(np.mean([r["psnr_plain"][0] for r in rows])),
         "plain_spp_to_40db_median": float(np.median([r["spp_to_40db"] for r in ok])) if ok else None,
@@ -250,6 +273,8 @@ def main():
     ap.add_argument("--eval", type=int, default=200)
     ap.add_argument("--steps", type=int, default=1500)
     ap.add_argument("--batch", type=int, default=16)
+    ap.add_argument("--input-spp", default="32,64",
+                    help="input sample counts of the training pairs, comma separated; the steps take them in turn")
     ap.add_argument("--out", default=str(HERE))
     ap.add_argument("--eval-only", default=None,
                     help="evaluate these weights (keeping the training record of the eval file in --out)")
@@ -279,25 +304,29 @@ def main():
     train_g = dataset(db, args.train, TRAIN_SEED0, 512, 512)
     log("training genomes", len(train_g), f"{time.perf_counter() - t0:.1f}s")
     t1 = time.perf_counter()
-    bins, base = dn.render_set(db, train_g, 512, 512, LOW_SPP, seed=1, both=True)
+    in_spp = [float(x) for x in args.input_spp.split(",")]
+    sets = [dn.render_set(db, train_g, 512, 512, sp, seed=1 + 10 * i, both=True) for i, sp in enumerate(in_spp)]
     tgt = dn.render_set(db, train_g, 512, 512, HIGH_SPP, seed=2, tonemap=True)
     torch.cuda.synchronize()
     render_s = time.perf_counter() - t1
     log("rendered training pairs", f"{render_s:.1f}s")
     nval = max(1, len(train_g) // 20)
     net = dn.denoiser(seed=1)
+    base = sets[0][1]
     val_plain = float(torch.mean((base[:nval, ..., :3] - tgt[:nval, ..., :3]) ** 2).item())
-    log("validation MSE of the plain 32-spp images", val_plain)
-    rep = dn.train(net, bins[nval:], base[nval:], tgt[nval:], LOW_SPP, args.steps, batch=args.batch,
-                   val=(bins[:nval], base[:nval], tgt[:nval]), log=log)
+    log(f"validation MSE of the plain {in_spp[0]:g}-spp images", val_plain)
+    rep = dn.train(net, [b[nval:] for b, _ in sets], [i[nval:] for _, i in sets], tgt[nval:], in_spp, args.steps,
+                   batch=args.batch, val=([b[:nval] for b, _ in sets], [i[:nval] for _, i in sets], tgt[:nval]),
+                   log=log)
     log("trained", rep)
     net.save(out / "denoiser_weights.npz")
-    del bins, base, tgt
+    del sets, base, tgt
     torch.cuda.empty_cache()
     eval_g = dataset(db, args.eval, EVAL_SEED0, 1920, 1080)
     log("evaluation genomes", len(eval_g))
     ev = evaluate(db, net, eval_g, 1920, 1080)
     ev["training"] = {"flames": len(train_g), "validation_flames": nval, "steps": rep.steps, "batch": args.batch,
+                      "input_spp": in_spp,
                       "seconds": rep.seconds, "ms_per_step": rep.ms_per_step, "first_loss": rep.first_loss,
                       "last_loss": rep.last_loss, "val_loss": rep.val_loss, "val_loss_plain_32spp": val_plain,
                       "render_seconds": render_s}

@@ -102,12 +102,44 @@ def test_batch_graph_replay(hetero):
         outs.append([b.bins(u).cpu().numpy().astype(np.float64) for u in range(len(units))])
     info = b.info()
     assert info["graph"] == 1
-    assert info["launches_per_run"] == 5 + 2 * len(units)
+    # fix_rotation once per independent flame (their samples are joined by no
+    # unit's segment), catmull, prepare, counter clear, iterate, then blur and
+    # tonemap per unit
+    assert info["launches_per_run"] == len(units) + 4 + 2 * len(units)
     # replays draw fresh random streams, and each starts from cleared histograms
     for u in range(len(units)):
         a, c = outs[0][u][..., 3], outs[1][u][..., 3]
         assert not np.array_equal(a, c)
         assert _l1(a, c) < 1.5 * _l1(outs[1][u][..., 3], outs[2][u][..., 3]) + 0.02
+
+
+def test_independent_flames_prepare_bit_identically(db):
+    """A batch of independent flames (each 4 copies of its own sample, unit i
+    on segment 4 i, t = 0, as the heterogeneous workload): every unit's
+    prepared parameter block equals, bit for bit, what the single-flame path
+    prepares from that flame's 4 samples alone (the screen offsets aside,
+    where the single-flame path adds its jitter). fix_rotation restarts its
+    angle unwrapping between samples that no unit's segment joins; unwrapped
+    across the flames, later flames' angles carried multiples of 2 pi into
+    FP32 and their affines differed in the last bits, enough to move the
+    render of a sensitive flame by more than its noise."""
+    fl = lr.align_flames(db, [lr.flame.from_json(db, syn.hd_flame(70 + i, n_xforms=2 + 3 * i, final=False))
+                              for i in range(4)])
+    k = lr.flame_compiler().get_flame_kernel(db, fl[0])
+    w, h = 96, 64
+    samples = np.concatenate([f.pack_samples(4, w, h).reshape(4, -1) for f in fl])
+    units = [lr.batch_unit(w, h, 1.0, segment=4 * i, t=0.0) for i in range(len(fl))]
+    b = lr.batch(k, units, samples.shape[0], out_format=-1)
+    b.set_samples(samples)
+    b.run()
+    b.wait()
+    R = fl[0].size_reals()
+    for u in range(len(fl)):
+        got = b.params(u).cpu().numpy()
+        want = k.prepare_samples(samples[4 * u:4 * u + 4], [0], [0.0])[0]
+        idx = np.r_[0:4, 6:got.size]
+        np.testing.assert_array_equal(got[idx], want[idx], err_msg=f"unit {u}")
+        assert R > 6
 
 
 def test_batch_prepare_matches_single_flame_prepare(db):

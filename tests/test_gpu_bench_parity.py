@@ -63,7 +63,15 @@ def test_bench_genome_at_1080p_matches_oracle(db):
         assert d < 1.25 * floor, (c, d, floor)
 
 
-def _check_units(k, units, al_of, samples_of, b1, b2, per, picks, seeds=(11, 12)):
+def _check_units(k, units, al_of, samples_of, b1, b2, per, picks, seeds=(11, 12, 13, 14)):
+    """Per unit: batch renders b1, b2 against individual plain renders of the
+    same genome with `seeds`. The single-flame path keeps one antialiasing
+    jitter per block for a whole render, so on flames with a few hot points
+    its seed-to-seed distance is dominated by a handful of random sub-pixel
+    shifts and varies a lot from pair to pair; distances are therefore means
+    over all pairs: fi over the individual pairs, d over (b1, individual)."""
+    import itertools
+
     for u in picks:
         U = units[u]
         w, h, spp = U.width, U.height, U.quality
@@ -78,9 +86,10 @@ def _check_units(k, units, al_of, samples_of, b1, b2, per, picks, seeds=(11, 12)
             ind.append(st.bins().cpu().numpy().astype(np.float64))
             del st
         for c in (3, 0):
-            fb, fi = _l1(got[..., c], got2[..., c]), _l1(ind[0][..., c], ind[1][..., c])
+            fb = _l1(got[..., c], got2[..., c])
+            fi = float(np.mean([_l1(a[..., c], b[..., c]) for a, b in itertools.combinations(ind, 2)]))
             floor = float(np.sqrt((fb * fb + fi * fi) / 2))
-            d = _l1(got[..., c], ind[0][..., c])
+            d = float(np.mean([_l1(got[..., c], a[..., c]) for a in ind]))
             assert d < 1.3 * floor, (u, (w, h, spp), c, d, fb, fi)
 
 
