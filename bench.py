@@ -538,8 +538,9 @@ def run_batch(args) -> dict:
 
 
 DENOISE_WORKLOAD = ("learned denoiser at 1920x1080: 32-spp render + U-Net (trained weights "
-                    "refraktor_gb300/workloads/denoiser_weights.npz), plain render as the fallback below 40 dB, vs the "
-                    "plain path's time to 40 dB PSNR against an independent 4096-spp render, seeded held-out flames")
+                    "refraktor_gb300/workloads/denoiser_weights.npz), then below 40 dB a 64-spp render + U-Net, then the "
+                    "plain render as the fallback, vs the plain path's time to 40 dB PSNR against an independent "
+                    "4096-spp render, seeded held-out flames")
 
 
 def run_denoise(args) -> dict:
