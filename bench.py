@@ -45,17 +45,18 @@ WORKLOAD = "plain 1080p single flame: 1920x1080, 1024 spp, 8 xforms + final xfor
 
 # dram__bytes_read.sum + dram__bytes_write.sum of one 1024-spp rfk_bin launch of
 # this workload at the bench's launch shape (608 x 256, 8 chains per thread,
-# flush 4, block sort, 4 blocks per SM; one ncu pass over the --ncu-case launch
-# at 1024 spp)
-BIN_DRAM_BYTES_PER_LAUNCH = 46.795264e6 + 12.903424e6
-# smsp__inst_executed.sum / chain steps of the same 1024-spp launch: 23.157 G
+# flush 4 with fixed-point hot-pixel sums, block sort, 4 blocks per SM; one ncu
+# pass over the --ncu-case launch at 1024 spp)
+BIN_DRAM_BYTES_PER_LAUNCH = 46816512 + 12792064
+# smsp__inst_executed.sum / chain steps of the same 1024-spp launch: 21.406 G
 # warp instructions for 2.168 G chain steps; each SM sub-partition issues one
 # warp instruction per clock
-BIN_WARP_INST_PER_ITER = 23156553057 / 2168324096
+BIN_WARP_INST_PER_ITER = 21405671974 / 2168061952
 # dram__bytes_read.sum + dram__bytes_write.sum of one rfk_bin_batch launch of
-# each batched workload (ncu, one pass over the bench's own batch launch);
-# None until captured
-BATCH_DRAM_BYTES_PER_RUN: dict = {"anim": None, "hetero": None}
+# each batched workload (ncu, one pass over the bench's first launch at the
+# chosen queue-item length, flush 4 at 608 x 256, 8 chains per thread)
+BATCH_DRAM_BYTES_PER_RUN: dict = {"anim": 1005712640 + 1424995072, "hetero": 769470464 + 1991087360}
+
 
 def _dist():
     ws = int(os.environ.get("WORLD_SIZE", "1"))
