@@ -136,22 +136,50 @@ def evaluate(db, net, genomes, w: int, h: int, seed: int = 7) -> dict:
 
 
 FALLBACK_CHECKPOINTS = [32, 48, 64, 96, 128, 192, 256, 384, 512, 768, 1024, 1536, 2048, 3072, 4096]
+# spp at which the denoised path runs the U-Net, in turn, before it falls back
+# to the plain render
+CASCADE_SPP = (32, 64, 128)
 
 
-def evaluate_with_fallback(db, net, genomes, w: int, h: int, seed: int = 7, kernel=None) -> dict:
+def cascade_time(row: dict, stages=CASCADE_SPP) -> float:
+    """Device time of one frame on the denoised path (cascade), from one
+    evaluation row: warm-up + bin to stages[0] + tonemap + U-Net; while the
+    frame is below 40 dB, continue the render to the next stage and tonemap -
+    done if the plain image reached 40 dB by then (the render stops at the
+    plain path's interpolated 40 dB spp, as the plain path's own time does) -
+    else run the U-Net again; below 40 dB after the last stage, continue the
+    plain render to its 40 dB spp and tonemap. Every stage is paid."""
+    spp, t_bin, t_tm, s40, tb40 = row["spp"], row["t_bin"], row["t_tonemap"], row["spp_to_40db"], row["tb40"]
+
+    def tb(sp):  # bin time to the checkpoint of sp spp
+        return t_bin[FALLBACK_CHECKPOINTS.index(sp)]
+
+    t = row["t_warmup"] + tb(stages[0]) + t_tm + row["t_unet_at"][str(stages[0])]
+    if row["psnr_denoised_at"][str(stages[0])] >= 40.0:
+        return t
+    prev = stages[0]
+    for sp in stages[1:]:
+        if s40 <= sp:
+            return t + max(tb40 - tb(prev), 0.0) + t_tm
+        t += tb(sp) - tb(prev) + t_tm + row["t_unet_at"][str(sp)]
+        if row["psnr_denoised_at"][str(sp)] >= 40.0:
+            return t
+        prev = sp
+    return t + max(tb40 - tb(prev), 0.0) + t_tm
+
+
+def evaluate_with_fallback(db, net, genomes, w: int, h: int, seed: int = 7, kernel=None,
+                           stages=CASCADE_SPP) -> dict:
     """Seconds per frame to 40 dB PSNR, denoised path against plain path, with
     the plain path as the denoised path's fallback. Per flame (device time
-    with CUDA events on the render stream):
+    with CUDA events on the render stream; one render state re-warmed per
+    frame, as a renderer drawing frame after frame keeps it):
       plain     warm-up + bin to the spp where the PSNR against an independent
                 4096-spp render first reaches 40 dB (interpolated on log2 spp
                 between checkpoints, the bin time likewise) + one tonemap;
-      denoised  a cascade, each stage paid in full: warm-up + bin to 32 spp
-                + tonemap + U-Net; a frame still below 40 dB continues its
-                render to 64 spp and tonemaps (done if the plain image reached
-                40 dB by 64 spp), else runs the U-Net again on the 64-spp
-                histogram; a frame below 40 dB after that continues the plain
-                render to the plain path's 40 dB spp and tonemaps again.
-      32 only   the same without the 64-spp stage (keys *_32_only).
+      denoised  the cascade of cascade_time over `stages` (U-Net at 32, 64,
+                128 spp in turn, then the plain render);
+      32 only   U-Net at 32 spp, then the plain render (keys *_32_only).
     Flames whose plain render stays below 40 dB at 4096 spp have no plain time
     and are left out of both means (counted in `plain_never_reaches`)."""
     import torch
@@ -169,6 +197,9 @@ def evaluate_with_fallback(db, net, genomes, w: int, h: int, seed: int = 7, kern
     img = torch.empty((h, w, 4), dtype=torch.float32, device="cuda")
     ref = torch.empty((h, w, 4), dtype=torch.float32, device="cuda")
     den = torch.empty((h, w, 4), dtype=torch.float32, device="cuda")
+    first = fs[0].pack_samples(4, w, h)
+    st = k.warmup(first, (w, h), seed=seed, count=20, stream=stream)
+    st_ref = k.warmup(first, (w, h), seed=seed + 1, count=20, stream=stream)
 
     def timed(fn):
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -178,92 +209,85 @@ def evaluate_with_fallback(db, net, genomes, w: int, h: int, seed: int = 7, kern
         e1.synchronize()
         return out, e0.elapsed_time(e1) / 1e3
 
+    last = max(stages)
     rows = []
     for i, f in enumerate(fs):
         tp = f.tonemap_params()
         tmargs = (tp["gamma"], tp["brightness"], tp["vibrancy"])
         samples = f.pack_samples(4, w, h)
-        st_ref = k.warmup(samples, (w, h), seed=seed + 2 * i + 1, count=20, stream=stream)
+        st_ref.rewarm(samples, seed=seed + 2 * i + 1, count=20, stream=stream)
         k.bin(st_ref, lr.bailout_args(iters=0, millis=0, quality=HIGH_SPP), stream=stream)
         tm.run(st_ref.bins(), ref, (w, h), st_ref.quality, *tmargs, fmt=lr.FLOAT4, stream=stream)
         stream.synchronize()
-        del st_ref
-        st, t_warm = timed(lambda: k.warmup(samples, (w, h), seed=seed + 2 * i, count=20, stream=stream))
+        _, t_warm = timed(lambda: st.rewarm(samples, seed=seed + 2 * i, count=20, stream=stream))
         _, t_tm = timed(lambda: tm.run(st.bins(), img, (w, h), 1.0, *tmargs, fmt=lr.FLOAT4, stream=stream))
-        spp, t_bin, psnrs, den_db, t_den, den64_db, den_vs_plain = [0.0], [0.0], [], None, None, None, None
-        t_den64 = None
+        spp, t_bin, psnrs, den_at, t_unet_at, den_vs_plain = [], [], [], {}, {}, None
         for c in FALLBACK_CHECKPOINTS:
             _, dt = timed(lambda: k.bin(st, lr.bailout_args(iters=0, millis=0, quality=c - st.quality), stream=stream))
             spp.append(st.quality)
-            t_bin.append(t_bin[-1] + dt)
+            t_bin.append((t_bin[-1] if t_bin else 0.0) + dt)
             tm.run(st.bins(), img, (w, h), st.quality, *tmargs, fmt=lr.FLOAT4, stream=stream)
             stream.synchronize()
             psnrs.append(dn.psnr(img, ref))
-            if c == FALLBACK_CHECKPOINTS[0]:
-                _, t_den = timed(lambda: net.denoise(st.bins(), img, den, st.quality, stream=stream))
-                den_db = dn.psnr(den, ref)
-                # no-reference: how far the U-Net moved the plain image
-                den_vs_plain = dn.psnr(den, img)
-            if c == 64:
-                _, t_den64 = timed(lambda: net.denoise(st.bins(), img, den, st.quality, stream=stream))
-                den64_db = dn.psnr(den, ref)
-            if psnrs[-1] >= 40.0 and c >= 64:
+            if c in stages:
+                _, t_unet_at[str(c)] = timed(lambda: net.denoise(st.bins(), img, den, st.quality, stream=stream))
+                den_at[str(c)] = dn.psnr(den, ref)
+                if c == stages[0]:
+                    # no-reference: how far the U-Net moved the plain image
+                    den_vs_plain = dn.psnr(den, img)
+            if psnrs[-1] >= 40.0 and c >= last:
                 break
-        row = {"psnr_denoised": den_db, "psnr_plain": psnrs, "spp": spp[1:], "t_warmup": t_warm, "t_tonemap": t_tm,
-               "t_unet": t_den, "t_bin_32": t_bin[1], "psnr_denoised_64": den64_db,
-               "psnr_denoised_vs_plain_32": den_vs_plain, "t_bin": t_bin[1:]}
+        row = {"psnr_denoised": den_at[str(stages[0])], "psnr_denoised_at": den_at, "t_unet_at": t_unet_at,
+               "psnr_plain": psnrs, "spp": spp, "t_warmup": t_warm, "t_tonemap": t_tm,
+               "t_unet": t_unet_at[str(stages[0])], "t_bin_first": t_bin[0], "t_bin": t_bin,
+               "psnr_denoised_vs_plain_first": den_vs_plain}
         if max(psnrs) >= 40.0:
             # the first checkpoint at or above 40 dB
             j = next(i for i, v in enumerate(psnrs) if v >= 40.0)
             if j == 0:
-                s40, tb40 = spp[1], t_bin[1]
+                s40, tb40 = spp[0], t_bin[0]
             else:
                 a, b = psnrs[j - 1], psnrs[j]
                 fr = (40.0 - a) / (b - a) if b > a else 1.0
-                s40 = float(2 ** (np.log2(spp[j]) + fr * (np.log2(spp[j + 1]) - np.log2(spp[j]))))
-                tb40 = t_bin[j] + fr * (t_bin[j + 1] - t_bin[j])
-            plain = t_warm + tb40 + t_tm
-            dpath = t_warm + t_bin[1] + t_tm + t_den
-            casc = dpath
-            if den_db < 40.0:
-                dpath += max(tb40 - t_bin[1], 0.0) + t_tm
-                # cascade: at 64 spp the plain image is done if it reached 40
-                # dB by then, else the U-Net runs again; then the plain render
-                i64 = FALLBACK_CHECKPOINTS.index(64) + 1
-                if s40 <= 64.0:
-                    casc += max(tb40 - t_bin[1], 0.0) + t_tm
-                else:
-                    casc += t_bin[i64] - t_bin[1] + t_tm + t_den64
-                    if den64_db < 40.0:
-                        casc += max(tb40 - t_bin[i64], 0.0) + t_tm
-            row.update(spp_to_40db=s40, plain_s=plain, denoised_s=dpath, cascade_s=casc)
+                s40 = float(2 ** (np.log2(spp[j - 1]) + fr * (np.log2(spp[j]) - np.log2(spp[j - 1]))))
+                tb40 = t_bin[j - 1] + fr * (t_bin[j] - t_bin[j - 1])
+            row.update(spp_to_40db=s40, tb40=tb40, plain_s=t_warm + tb40 + t_tm)
+            row["denoised_s"] = cascade_time(row, stages[:1])
+            row["cascade_s"] = cascade_time(row, stages)
         rows.append(row)
-        del st
+    del st, st_ref
     ok = [r for r in rows if "plain_s" in r]
     plain = np.array([r["plain_s"] for r in ok])
     dpath = np.array([r["denoised_s"] for r in ok])
     casc = np.array([r["cascade_s"] for r in ok])
-    pden = np.array([r["psnr_denoised"] for r in rows])
-    pden64 = np.array([r["psnr_denoised_64"] for r in rows])
     out = {
         "flames": len(rows), "width": w, "height": h, "plain_never_reaches": len(rows) - len(ok),
+        "cascade_spp": list(stages),
         "s_per_frame_to_40db_plain": float(plain.mean()) if ok else None,
         "s_per_frame_to_40db_denoised": float(casc.mean()) if ok else None,
         "speedup": float(plain.mean() / casc.mean()) if ok else None,
         "speedup_per_flame_median": float(np.median(plain / casc)) if ok else None,
         "s_per_frame_to_40db_denoised_32_only": float(dpath.mean()) if ok else None,
         "speedup_32_only": float(plain.mean() / dpath.mean()) if ok else None,
-        "denoised_reaches_40db": float((pden >= 40.0).mean()),
-        "denoised_64_reaches_40db": float((pden64 >= 40.0).mean()),
-        "cascade_reaches_40db_by_64spp": float(np.mean([(a >= 40.0) or (b >= 40.0) or r.get("spp_to_40db", 1e9) <= 64.0
-                                                        for a, b, r in zip(pden, pden64, rows)])),
-        "denoised_psnr_db_mean": float(pden.mean()), "denoised_psnr_db_median": float(np.median(pden)),
         "plain_psnr_db_32spp_mean": float(np.mean([r["psnr_plain"][0] for r in rows])),
         "plain_spp_to_40db_median": float(np.median([r["spp_to_40db"] for r in ok])) if ok else None,
         "unet_ms_median": 1e3 * float(np.median([r["t_unet"] for r in rows])),
-        "render_32spp_ms_median": 1e3 * float(np.median([r["t_bin_32"] + r["t_warmup"] + r["t_tonemap"] for r in rows])),
+        "warmup_ms_median": 1e3 * float(np.median([r["t_warmup"] for r in rows])),
+        "render_first_stage_ms_median": 1e3 * float(np.median([r["t_bin_first"] + r["t_warmup"] + r["t_tonemap"]
+                                                               for r in rows])),
         "per_flame": rows,
     }
+    for sp in stages:
+        pd = np.array([r["psnr_denoised_at"][str(sp)] for r in rows])
+        out[f"denoised_{sp}spp_reaches_40db"] = float((pd >= 40.0).mean())
+        out[f"denoised_{sp}spp_psnr_db_mean"] = float(pd.mean())
+    # frames done by the end of each stage (denoised or plain image at 40 dB)
+    for n in range(1, len(stages) + 1):
+        out[f"cascade_done_by_{stages[n - 1]}spp"] = float(np.mean([
+            any(r["psnr_denoised_at"][str(sp)] >= 40.0 for sp in stages[:n]) or r.get("spp_to_40db", 1e9) <= stages[n - 1]
+            for r in rows]))
+    out["denoised_reaches_40db"] = out[f"denoised_{stages[0]}spp_reaches_40db"]
+    out["denoised_psnr_db_mean"] = out[f"denoised_{stages[0]}spp_psnr_db_mean"]
     return out
 
 
