@@ -5,8 +5,8 @@ against the plain path (the learned-denoiser workload):
                (8 xforms, Dirichlet(1) weights, final xform, 1-3 variations
                each from the 14-variation set), visibility-rejected and framed
                at 512 x 512; input: the 32-spp histogram and its tonemapped
-               image, and in turn the 64-spp ones (--input-spp; the network's
-               log-spp channel tells them apart), target: the tonemapped
+               image, and in turn the 64- and 128-spp ones (--input-spp; the
+               network's log-spp channel tells them apart), target: the tonemapped
                4096-spp render; Adam, lr 1e-3 (cosine decay), batch 16,
                random mirroring
   evaluation   `--eval` held-out seeded flames at 1920 x 1080: the plain path
@@ -297,7 +297,7 @@ def main():
     ap.add_argument("--eval", type=int, default=200)
     ap.add_argument("--steps", type=int, default=1500)
     ap.add_argument("--batch", type=int, default=16)
-    ap.add_argument("--input-spp", default="32,64",
+    ap.add_argument("--input-spp", default="32,64,128",
                     help="input sample counts of the training pairs, comma separated; the steps take them in turn")
     ap.add_argument("--out", default=str(HERE))
     ap.add_argument("--eval-only", default=None,
