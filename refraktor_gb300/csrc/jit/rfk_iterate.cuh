@@ -376,29 +376,36 @@ __device__ __forceinline__ void rfk_sort_chains(float4* __restrict__ region, con
 #define RFK_NW (RFK_BLOCK / 32)
 // Block-wide counting sort of the block's RFK_BLOCK * RFK_CPT chains by picked
 // xform (deterministic order: xform-major, then warp, then round, then lane),
-// in place in the chain array: every thread has read its own slots (values v,
-// picks k) before the call, and the scatter comes after a barrier. Two
-// barriers per pass: after the first, every warp derives the starts it needs
-// from the per-(xform, warp) counters itself (no single-warp scan and second
-// barrier). counts[RFK_NX * RFK_NW] must be zero on entry. `next` (the other
-// counter set) is cleared after the first barrier: every warp read it in the
-// previous pass before that pass's second barrier, and its next-pass updates
-// come after this pass's second barrier. Afterwards slot q * RFK_BLOCK + t
-// holds thread t's round-q chain, so a warp's round covers 32 consecutive
-// slots of one xform run except at run ends.
-__device__ __forceinline__ void rfk_block_sort(float4* __restrict__ chains, const float4 (&v)[RFK_CPT],
-                                               const int (&k)[RFK_CPT], const unsigned (&bits)[RFK_CPT],
+// in place in the chain array: every thread has read its own slots (positions
+// and colours v, picks) before the call, and the scatter comes after a
+// barrier. Two barriers per pass: after the first, every warp derives the
+// starts it needs from the per-(xform, warp) counters itself (no single-warp
+// scan and second barrier). counts[RFK_NX * RFK_NW] must be zero on entry.
+// `next` (the other counter set) is cleared after the first barrier: every
+// warp read it in the previous pass before that pass's second barrier, and its
+// next-pass updates come after this pass's second barrier. Afterwards slot
+// q * RFK_BLOCK + t holds thread t's round-q chain, so a warp's round covers 32
+// consecutive slots of one xform run except at run ends.
+// kb[q / 2] holds round q's pick | 8 spare random bits << 8 in its 16-bit half
+// q % 2, and the offsets are packed the same way: two per register, so the
+// sort of 8 chains per thread holds 24 + 4 + 4 registers instead of 24 + 24
+// (fewer spills at the 64-register cap; 1.3% faster on the 1080p genome).
+__device__ __forceinline__ void rfk_block_sort(float4* __restrict__ chains, const float3 (&v)[RFK_CPT],
+                                               const unsigned (&kb)[(RFK_CPT + 1) / 2],
                                                unsigned* __restrict__ counts, unsigned* __restrict__ next) {
     const unsigned lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
     const unsigned lt = (1u << lane) - 1u;
-    unsigned off[RFK_CPT];
+    unsigned offp[(RFK_CPT + 1) / 2];
 #pragma unroll
     for (int q = 0; q < RFK_CPT; q++) {
-        const unsigned same = __match_any_sync(0xffffffffu, k[q]);
+        const int k = (int)((kb[q >> 1] >> (16 * (q & 1))) & 0xFFu);
+        const unsigned same = __match_any_sync(0xffffffffu, k);
         const int leader = __ffs(same) - 1;
         unsigned base = 0;
-        if ((int)lane == leader) base = atomicAdd(&counts[k[q] * RFK_NW + warp], (unsigned)__popc(same));
-        off[q] = __shfl_sync(0xffffffffu, base, leader) + __popc(same & lt);
+        if ((int)lane == leader) base = atomicAdd(&counts[k * RFK_NW + warp], (unsigned)__popc(same));
+        const unsigned off = __shfl_sync(0xffffffffu, base, leader) + __popc(same & lt);
+        if (q & 1) offp[q >> 1] |= off << 16;
+        else offp[q >> 1] = off;
     }
     __syncthreads();
     for (unsigned i = threadIdx.x; i < RFK_NX * RFK_NW; i += RFK_BLOCK) next[i] = 0u;
@@ -423,8 +430,10 @@ __device__ __forceinline__ void rfk_block_sort(float4* __restrict__ chains, cons
     const unsigned start = incl - tot + part;
 #pragma unroll
     for (int q = 0; q < RFK_CPT; q++) {
-        const unsigned pos = __shfl_sync(0xffffffffu, start, k[q]) + off[q];
-        chains[pos] = make_float4(v[q].x, v[q].y, v[q].z, __int_as_float(k[q] | (int)(bits[q] << 8)));
+        const unsigned kbq = (kb[q >> 1] >> (16 * (q & 1))) & 0xFFFFu;
+        const unsigned pos =
+            __shfl_sync(0xffffffffu, start, (int)(kbq & 0xFFu)) + ((offp[q >> 1] >> (16 * (q & 1))) & 0xFFFFu);
+        chains[pos] = make_float4(v[q].x, v[q].y, v[q].z, __int_as_float((int)kbq));
     }
     __syncthreads();
 }
@@ -827,6 +836,22 @@ __device__ __forceinline__ void rfk_pick_sort(rfk_pass_smem& sm, const float* P,
 #if RFK_SORT
     Rng pr;
     pr.start_lazy(lane_stream, call_id, pass, seed, salt ^ 0x9E3779B9u);
+#if RFK_SORT == 2
+    float3 v3[RFK_CPT];
+    unsigned kb[(RFK_CPT + 1) / 2];
+#pragma unroll
+    for (int q = 0; q < RFK_CPT; q++) {
+        // the pick takes the top 24 bits of its word; the low 8 go with the
+        // chain to its move (Rng::give_bits)
+        const float4 c4 = sm.chains[rfk_slot(q)];
+        v3[q] = make_float3(c4.x, c4.y, c4.z);
+        const rfk_u32 u = pr.next();
+        const unsigned kbq = (unsigned)rfk_pick(rfk_u01f(u), P, (unsigned)__float_as_int(c4.w)) | ((u & 0xFFu) << 8);
+        if (q & 1) kb[q >> 1] |= kbq << 16;
+        else kb[q >> 1] = kbq;
+    }
+    rfk_block_sort(sm.chains, v3, kb, sm.counts[pass & 1], sm.counts[(pass + 1) & 1]);
+#else
     float4 v[RFK_CPT];
     int kk[RFK_CPT];
     unsigned bits[RFK_CPT];
@@ -834,14 +859,9 @@ __device__ __forceinline__ void rfk_pick_sort(rfk_pass_smem& sm, const float* P,
     for (int q = 0; q < RFK_CPT; q++) {
         v[q] = sm.chains[rfk_slot(q)];
         const rfk_u32 u = pr.next();
-        // the pick takes the top 24 bits; the low 8 go with the chain to its
-        // move (Rng::give_bits)
         kk[q] = rfk_pick(rfk_u01f(u), P, (unsigned)__float_as_int(v[q].w));
         bits[q] = u & 0xFFu;
     }
-#if RFK_SORT == 2
-    rfk_block_sort(sm.chains, v, kk, bits, sm.counts[pass & 1], sm.counts[(pass + 1) & 1]);
-#else
     rfk_sort_chains(sm.chains + (threadIdx.x & ~31u) * RFK_CPT, v, kk, bits, sm.counts[threadIdx.x >> 5]);
 #endif
 #else
