@@ -158,6 +158,10 @@ extern "C" __global__ void __launch_bounds__(256) rfk_prepare(const float4* __re
     __shared__ float P[RFK_SAMPLE_FLOATS];
     const unsigned s = blockIdx.x;
     const float t = t_of[s];
+    // the padding after the reals and before the palette is written too (as
+    // 0): every float of the block that leaves this kernel is defined
+    for (unsigned i = RFK_SIZE_REALS + threadIdx.x; i < RFK_OFF_ALIAS; i += blockDim.x) P[i] = 0.0f;
+    for (unsigned i = RFK_OFF_PAL_RAW + threadIdx.x; i < RFK_OFF_PAL; i += blockDim.x) P[i] = 0.0f;
     const float4* seg = coeff + (size_t)seg_of[s] * sample_size;
 
     // Hermite basis of the segment p1 -> p2 with tangents m1, m2 (the same

@@ -284,6 +284,30 @@ def test_warmup_adopts_the_callers_histogram(db, comp):
         k.warmup(samples, torch.ones((h, w, 3), dtype=torch.float32, device="cuda"), seed=9, count=1)
 
 
+def test_prepared_blocks_are_finite_and_repeatable(db, comp):
+    """Every float of a prepared parameter block is defined: the padding after
+    the reals (an odd count) and before the 16-byte aligned palette is 0, and
+    two identical calls give the same bits (the blocks feed the bin kernels,
+    the batch and the allocation-free entry point alike)."""
+    g = syn.hd_flame(4)
+    f = lr.flame.from_json(db, g)
+    k = comp.get_flame_kernel(db, f)
+    samples = f.pack_samples(4, 320, 180)
+    seg, t = [0, 0, 0, 0], [0.0, 0.3, 0.6, 0.9]
+    a = k.prepare_samples(samples, seg, t, seed=3)
+    b = k.prepare_samples(samples, seg, t, seed=3)
+    assert np.all(np.isfinite(a))
+    np.testing.assert_array_equal(a.view(np.uint32), b.view(np.uint32))
+    R = f.size_reals()
+    pal0 = k.info["sample_floats"] - 1024
+    if R % 2:
+        assert np.all(a[:, R] == 0.0)
+    # the floats between the pick tables and the palette (alignment padding)
+    nx = k.info["num_xforms"]
+    end_tables = (R + 1) // 2 * 2 + 2 * nx + (2 * nx * nx if k.info["chaos"] else 0)
+    assert np.all(a[:, end_tables:pal0] == 0.0)
+
+
 def test_prepared_flame_matches_oracle_interpolation(db, comp):
     """Row a3/a4: FP32 Catmull-Rom + polar affines + 8-bit palette vs FP64."""
     rng = np.random.default_rng(11)
