@@ -47,11 +47,11 @@ WORKLOAD = "plain 1080p single flame: 1920x1080, 1024 spp, 8 xforms + final xfor
 # this workload at the bench's launch shape (608 x 256, 8 chains per thread,
 # flush 4 with fixed-point hot-pixel sums, block sort, 4 blocks per SM; one ncu
 # pass over the --ncu-case launch at 1024 spp)
-BIN_DRAM_BYTES_PER_LAUNCH = 46816512 + 12792064
-# smsp__inst_executed.sum / chain steps of the same 1024-spp launch: 21.406 G
+BIN_DRAM_BYTES_PER_LAUNCH = 46690816 + 1081344
+# smsp__inst_executed.sum / chain steps of the same 1024-spp launch: 21.736 G
 # warp instructions for 2.168 G chain steps; each SM sub-partition issues one
 # warp instruction per clock
-BIN_WARP_INST_PER_ITER = 21405671974 / 2168061952
+BIN_WARP_INST_PER_ITER = 21736283626 / 2168258560
 # dram__bytes_read.sum + dram__bytes_write.sum of one rfk_bin_batch launch of
 # each batched workload (ncu, one pass over the bench's first launch at the
 # chosen queue-item length, flush 4 at 608 x 256, 8 chains per thread)
