@@ -258,22 +258,25 @@ def run_gpu(args) -> dict:
     tmap = lr.tonemapper()
     e2e_times = []
     e2e_passes = 0
-    for i in range(args.warmup + args.steps):
-        _flush_l2(flush)
-        torch.cuda.synchronize()
-        t0 = time.perf_counter()
-        s2.rewarm(samples, seed=100 + i, count=WARMUP_PASSES, stream=stream)
-        r = k.bin(s2, bo, stream=stream)
-        with torch.cuda.stream(stream):
-            lr.density_blur(s2.bins(), blurred, (W, H), 9.0, 0.0, 0.5, stream=stream)
-            tmap.run(blurred, img, (W, H), s2.quality, tp["gamma"], tp["brightness"], tp["vibrancy"], fmt=lr.HALF4,
-                     stream=stream)
-            out_host.copy_(img, non_blocking=True)
-        stream.synchronize()
-        dt = time.perf_counter() - t0
-        if i >= args.warmup:
-            e2e_times.append(dt)
-            e2e_passes += r.total_passes  # bin iterations only; the warm-up passes count as time
+    e2e_bin_s = 0.0
+    with ClockSampler(int(os.environ.get("LOCAL_RANK", "0"))) as e2e_clocks:
+        for i in range(args.warmup + args.steps):
+            _flush_l2(flush)
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            s2.rewarm(samples, seed=100 + i, count=WARMUP_PASSES, stream=stream)
+            r = k.bin(s2, bo, stream=stream)
+            with torch.cuda.stream(stream):
+                lr.density_blur(s2.bins(), blurred, (W, H), 9.0, 0.0, 0.5, stream=stream)
+                tmap.run(blurred, img, (W, H), s2.quality, tp["gamma"], tp["brightness"], tp["vibrancy"],
+                         fmt=lr.HALF4, stream=stream)
+                out_host.copy_(img, non_blocking=True)
+            stream.synchronize()
+            dt = time.perf_counter() - t0
+            if i >= args.warmup:
+                e2e_times.append(dt)
+                e2e_passes += r.total_passes  # bin iterations only; the warm-up passes count as time
+                e2e_bin_s += r.elapsed_ms / 1e3
     e2e_t = sum(e2e_times)
     e2e_t, (e2e_passes,) = merge_ranks(e2e_t, [e2e_passes])
 
@@ -296,7 +299,8 @@ def run_gpu(args) -> dict:
                    "autotune": tune_report, "l2": "512 MiB buffer written between timed steps",
                    "parallelism": f"replicas x{ws}"},
         "e2e": {"value": e2e_passes / e2e_t, "unit": "iterations/s", "s_per_frame": e2e_t / args.steps,
-                "h2d_bytes_per_step": int(samples.nbytes), "d2h_bytes_per_step": int(W * H * 4 * 2)},
+                "h2d_bytes_per_step": int(samples.nbytes), "d2h_bytes_per_step": int(W * H * 4 * 2),
+                "bin_kernel_ms_per_frame": 1e3 * e2e_bin_s / args.steps, "clocks": e2e_clocks.summary()},
         "roofline": {"bound": "l2_atomic", "achieved": achieved_ops * 16 / 1e9, "peak": peak_ops * 16 / 1e9,
                      "unit": "GB/s", "frac": achieved_ops / peak_ops, "traffic": BIN_DRAM_BYTES_PER_LAUNCH,
                      "achieved_ops": achieved_ops, "peak_ops": peak_ops,
@@ -308,6 +312,7 @@ def run_gpu(args) -> dict:
         "clocks": csum,
         "draws_per_s": draws / t_total,
         "bin_ms": 1e3 * bin_launch_s,
+        "bin_kernel_ms": 1e3 * elapsed_kernel / args.steps,
         "registers": info["registers"],
     }
     if rank == 0 and not args.no_cpu_baseline:
