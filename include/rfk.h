@@ -105,9 +105,11 @@ typedef struct {
     int chains_per_thread; /* 0 = 4 when sorting, else 1 */
     int flush;             /* histogram update: 0 = red.global.add.v4.f32 per draw, 1 = warp-aggregated,
                               2 = warp-aggregated into a per-block shared-memory cache of hot pixels,
-                              3 = the shared-memory cache without warp aggregation, 4 = shared-memory
-                              sums for the pixels the block's own draws show to be hot, one red per
-                              draw elsewhere */
+                              3 = the shared-memory cache without warp aggregation, 4 = fixed-point
+                              shared-memory sums for the pixels the block's own draws show to be hot,
+                              one red per draw elsewhere. 0 and 3 add draws one at a time, so a
+                              pixel's FP32 sum stops at 2^24 (adding 1 there rounds back); the
+                              autotuner picks among 1, 2 and 4 only */
     int blocks_per_sm;     /* 0 = registers capped so that 1280 / block bin blocks fit per SM, and as
                               many run as fit; n > 0 = registers capped so that n fit, and at most n
                               run per SM (launch bounds) */
