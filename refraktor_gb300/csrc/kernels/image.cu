@@ -92,8 +92,10 @@ __global__ void __launch_bounds__(DE_TILE_X * DE_TILE_Y / 2) de_blur_kernel(cons
     __shared__ float4 tile[DE_SH][DE_SW];
     __shared__ unsigned char lv[DE_SH][DE_SW];
     __shared__ float2 tab[RFK_DE_LEVELS];  // (1 / (r + 1)^2, 1 / Z(r)) per level
+    __shared__ int max_rc;                  // largest support radius of a source in the tile
     const int tx0 = blockIdx.x * DE_TILE_X - DE_HALO, ty0 = blockIdx.y * DE_TILE_Y - DE_HALO;
     const int nthreads = blockDim.x;
+    if (threadIdx.x == 0) max_rc = 0;
     for (int l = threadIdx.x; l < RFK_DE_LEVELS; l += nthreads) {
         const float r = (float)l / RFK_DE_STEPS;
         const float a = 1.0f / ((r + 1.0f) * (r + 1.0f));
@@ -103,6 +105,8 @@ __global__ void __launch_bounds__(DE_TILE_X * DE_TILE_Y / 2) de_blur_kernel(cons
             for (int ox = -rc; ox <= rc; ox++) z += fmaxf(0.0f, 1.0f - (float)(ox * ox + oy * oy) * a);
         tab[l] = make_float2(a, 1.0f / z);
     }
+    __syncthreads();  // max_rc cleared
+    int my_rc = 0;
     for (int i = threadIdx.x; i < DE_SW * DE_SH; i += nthreads) {
         const int sy = i / DE_SW, sx = i % DE_SW;
         const int gx = tx0 + sx, gy = ty0 + sy;
@@ -114,8 +118,14 @@ __global__ void __launch_bounds__(DE_TILE_X * DE_TILE_Y / 2) de_blur_kernel(cons
         }
         tile[sy][sx] = v;
         lv[sy][sx] = l;
+        if (l != 255) my_rc = max(my_rc, ((int)l + RFK_DE_STEPS - 1) / RFK_DE_STEPS);
     }
+    if (my_rc > 0) atomicMax(&max_rc, my_rc);
     __syncthreads();
+    // no source of the tile (halo included) reaches further than max_rc, so
+    // the offsets beyond it would all be skipped below: the loop stops there
+    // (an empty tile writes zeros at once); the sum is unchanged bit for bit
+    reach = min(reach, max_rc);
     // two output pixels per thread, rows y and y + DE_TILE_Y/2
     const int ox = threadIdx.x % DE_TILE_X, oy = threadIdx.x / DE_TILE_X;
     for (int half = 0; half < 2; half++) {

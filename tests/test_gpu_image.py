@@ -142,6 +142,38 @@ def test_density_blur_matches_oracle(max_r, min_r, curve):
     assert got[..., 3].sum() <= bins[..., 3].sum() * (1 + 1e-5)
 
 
+def test_density_blur_patchy_image_matches_oracle():
+    """A render's usual layout: most tiles empty, dense regions (small blur
+    radius), and isolated faint pixels (the full 9-pixel radius) near the
+    edges of empty tiles. Each block loops only as far as the widest support
+    of the sources in its tile and halo; the result must equal the scatter
+    definition everywhere, also where a faint pixel's support reaches into an
+    otherwise empty tile."""
+    rng = np.random.default_rng(9)
+    h, w = 150, 260
+    dens = np.zeros((h, w), np.float32)
+    yy, xx = np.mgrid[0:h, 0:w]
+    for cy, cx, r in ((40, 60, 18), (110, 200, 12)):
+        blob = (yy - cy) ** 2 + (xx - cx) ** 2 < r * r
+        dens[blob] = rng.uniform(50, 400, size=blob.sum()).astype(np.float32)
+    for _ in range(40):
+        dens[rng.integers(0, h), rng.integers(0, w)] = rng.uniform(0.5, 2.0)
+    col = rng.uniform(0, 1, size=(h, w, 3)).astype(np.float32)
+    bins = np.ascontiguousarray(np.concatenate([col * dens[..., None], dens[..., None]], axis=-1), dtype=np.float32)
+    d_in = torch.from_numpy(bins).cuda()
+    d_out = torch.empty_like(d_in)
+    lr.density_blur(d_in, d_out, (w, h), 9.0, 0.0, 0.5)
+    got = d_out.cpu().numpy().astype(np.float64)
+    ref = orc.density_blur(bins, 9.0, 0.0, 0.5)
+    err = np.abs(got - ref)
+    assert np.all(err <= 1e-5 * np.abs(ref) + 1e-6 * np.abs(ref).max()), float(err.max())
+    # the empty tiles far from every source stay exactly 0
+    far = np.ones((h, w), bool)
+    for y, x in zip(*np.nonzero(dens)):
+        far[max(0, y - 10):y + 11, max(0, x - 10):x + 11] = False
+    assert far.any() and np.all(got[far] == 0.0)
+
+
 T_VALUES = [0.0, 0.1, 0.25, 0.5, 0.77, 0.999, 1.0]
 
 
