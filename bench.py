@@ -328,7 +328,7 @@ def denoise_leg(db, flames: int) -> dict:
     """The second half of the metric: s/frame to 40 dB PSNR at 1920x1080,
     denoised path (render + U-Net) against the plain path, on `flames`
     held-out seeded flames of the 1080p workload's distribution: the denoised
-    path is a cascade (U-Net at 32, 64, 128 spp in turn, then the plain render
+    path is a cascade (U-Net at 32, 64, 96, 128 spp in turn, then the plain render
     as the fallback of every frame still below 40 dB), with the single-attempt
     figures beside it (refraktor_gb300/workloads/train_denoiser.py:
     evaluate_with_fallback). Device time per frame; rank 0 only."""
@@ -544,9 +544,9 @@ def run_batch(args) -> dict:
 
 
 DENOISE_WORKLOAD = ("learned denoiser at 1920x1080: 32-spp render + U-Net (trained weights "
-                    "refraktor_gb300/workloads/denoiser_weights.npz), then below 40 dB 64- and 128-spp renders + U-Net, "
-                    "then the plain render as the fallback, vs the plain path's time to 40 dB PSNR against an independent "
-                    "4096-spp render, seeded held-out flames")
+                    "refraktor_gb300/workloads/denoiser_weights.npz), then below 40 dB 64-, 96- and 128-spp "
+                    "renders + U-Net, then the plain render as the fallback, vs the plain path's time to 40 dB PSNR "
+                    "against an independent 4096-spp render, seeded held-out flames")
 
 
 def run_denoise(args) -> dict:
@@ -554,7 +554,7 @@ def run_denoise(args) -> dict:
     path renders progressively until its PSNR against an independent 4096-spp
     render crosses 40 dB (spp and time interpolated on log2 spp); the denoised
     path renders 32 spp and runs the U-Net, a frame left below 40 dB continues
-    to 64, then 128 spp and runs the U-Net again at each (unless its plain
+    to 64, 96, then 128 spp and runs the U-Net again at each (unless its plain
     image reached 40 dB), and a frame still below 40 dB continues the plain
     render to the plain path's 40 dB spp; every stage is paid. `value` is the denoised path's mean
     device time per frame with that cascade; the plain path's is beside it,
