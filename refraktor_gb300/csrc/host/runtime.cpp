@@ -981,13 +981,20 @@ rfk_status rfk_probe_red_v4(size_t bytes, uint32_t iters, double* ops_per_s) {
         const unsigned blocks = (unsigned)device_sm_count() * 8, threads = 256;
         cudaEvent_t a = cs.event(), b = cs.event();
         cuda_check(rfk_launch_red_v4_probe(buf, bytes / 16, iters, blocks, threads, nullptr), "probe");
-        cudaEventRecord(a);
-        cuda_check(rfk_launch_red_v4_probe(buf, bytes / 16, iters, blocks, threads, nullptr), "probe");
-        cudaEventRecord(b);
-        cuda_check(cudaEventSynchronize(b), "probe");
-        float ms = 0;
-        cuda_check(cudaEventElapsedTime(&ms, a, b), "probe timing");
-        *ops_per_s = (double)blocks * threads * iters / (ms * 1e-3);
+        // the median of 5 timed launches: one launch of this size takes under
+        // a millisecond, and single timings scattered by about 2%
+        std::vector<float> times;
+        for (int rep = 0; rep < 5; rep++) {
+            cudaEventRecord(a);
+            cuda_check(rfk_launch_red_v4_probe(buf, bytes / 16, iters, blocks, threads, nullptr), "probe");
+            cudaEventRecord(b);
+            cuda_check(cudaEventSynchronize(b), "probe");
+            float ms = 0;
+            cuda_check(cudaEventElapsedTime(&ms, a, b), "probe timing");
+            times.push_back(ms);
+        }
+        std::sort(times.begin(), times.end());
+        *ops_per_s = (double)blocks * threads * iters / (times[times.size() / 2] * 1e-3);
     });
 }
 
