@@ -718,9 +718,37 @@ def run_ncu_case(args) -> None:
     print(json.dumps({"ncu_case": k.info, "opts": opts, "passes": r.total_passes, "ms": r.elapsed_ms}))
 
 
+def run_ncu_batch(args) -> None:
+    """Small case for ncu captures of rfk_bin_batch: the first 8 flames of the
+    heterogeneous workload (one union-of-variations kernel, the autotuner's
+    launch shape for the workload) at 32 spp each, one batch run (a few tens
+    of MB on the device)."""
+    import dataclasses
+
+    from refraktor_gb300 import build
+    from refraktor_gb300 import librefrakt as lr
+
+    build.build()
+    db = lr.flamedb()
+    kf, samples, units, _, (tf, tsamples, tdims) = batch_workload(lr, db, "hetero")
+    opts, _ = lr.autotune(db, tf, tsamples, tdims)
+    k = lr.flame_compiler().get_flame_kernel(db, kf, **opts)
+    ss = kf.sample_size()
+    units = [dataclasses.replace(u, quality=32.0) for u in units[:8]]
+    smp = np.asarray(samples, dtype=np.float64).reshape(-1, ss)[:4 * len(units)]
+    b = lr.batch(k, units, smp.shape[0], passes_per_item=128, warmup=WARMUP_PASSES, out_format=-1)
+    b.set_samples(smp)
+    b.run()
+    tot, _ = b.wait()
+    print(json.dumps({"ncu_batch": k.info, "opts": opts, "units": [(u.width, u.height) for u in units],
+                      "passes": tot.total_passes, "ms": tot.elapsed_ms}))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--ncu-case", action="store_true")
+    ap.add_argument("--ncu-batch", action="store_true",
+                    help="small case for profiler captures of rfk_bin_batch (8 heterogeneous flames, 32 spp)")
     ap.add_argument("--ncu-launches", type=int, default=2)
     ap.add_argument("--ncu-spp", type=int, default=16)
     ap.add_argument("--flush", type=int, default=None)
@@ -752,6 +780,9 @@ def main():
               file=sys.stderr)
     if args.ncu_case:
         run_ncu_case(args)
+        return
+    if args.ncu_batch:
+        run_ncu_batch(args)
         return
     if args.impl == "reference":
         line = run_reference(args)
