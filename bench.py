@@ -258,7 +258,6 @@ def run_gpu(args) -> dict:
     out_host = torch.empty((H, W, 4), dtype=torch.float16, pin_memory=True)
     blurred = torch.empty((H, W, 4), dtype=torch.float32, device="cuda")
     img = torch.empty((H, W, 4), dtype=torch.float16, device="cuda")
-    s2 = st
     tmap = lr.tonemapper()
     e2e_times = []
     e2e_passes = 0
@@ -268,11 +267,11 @@ def run_gpu(args) -> dict:
             _flush_l2(flush)
             torch.cuda.synchronize()
             t0 = time.perf_counter()
-            s2.rewarm(samples, seed=100 + i, count=WARMUP_PASSES, stream=stream)
-            r = k.bin(s2, bo, stream=stream)
+            st.rewarm(samples, seed=100 + i, count=WARMUP_PASSES, stream=stream)
+            r = k.bin(st, bo, stream=stream)
             with torch.cuda.stream(stream):
-                lr.density_blur(s2.bins(), blurred, (W, H), 9.0, 0.0, 0.5, stream=stream)
-                tmap.run(blurred, img, (W, H), s2.quality, tp["gamma"], tp["brightness"], tp["vibrancy"],
+                lr.density_blur(st.bins(), blurred, (W, H), 9.0, 0.0, 0.5, stream=stream)
+                tmap.run(blurred, img, (W, H), st.quality, tp["gamma"], tp["brightness"], tp["vibrancy"],
                          fmt=lr.HALF4, stream=stream)
                 out_host.copy_(img, non_blocking=True)
             stream.synchronize()
